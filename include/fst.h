@@ -1,0 +1,203 @@
+/*
+ * fst.h — C ABI of libfst, the GB300 (sm_103a) implementation of FIESTA's
+ * per-Runge-Kutta-stage right-hand side and update for uniform Cartesian
+ * grids (the cart2d / cart3d modules).
+ *
+ * Everything crossing this boundary is plain C: a config struct, pointers and
+ * sizes.  No C++, Kokkos or torch types appear in any signature.
+ *
+ * State layout (host and device buffers alike): the layout FIESTA's CUDA build
+ * gives `FS4D var(ngi, ngj, ngk, nvt)` (Kokkos LayoutLeft, i fastest):
+ *
+ *     U[i + ngi*(j + ngj*(k + ngk*v))]     ngi = nci + 2*ng, ngk = 1 in 2D
+ *
+ * with ng = 3 ghost layers.  Variable order follows the reference:
+ *   3D: x-, y-, z-momentum, total energy, ns species densities, then (ceq) the
+ *       five C-equation variables C, C_hat, C_1, C_2, C_3
+ *       (src/cart3d.cpp:98-110 of the reference);
+ *   2D: x-, y-momentum, energy, ns species densities, then (ceq) C, C_hat,
+ *       Tau_1, Tau_2, Debug (src/cart2d.cpp:40-58).
+ *
+ * Every function returns FST_OK (0) or a negative status; fst_last_error()
+ * gives the message.  The reference calls exit(EXIT_FAILURE) instead
+ * (src/bc.cpp:266-268, src/luaReader.cpp:100-101).
+ *
+ * Threading: one context per host thread; all work is ordered on the
+ * context's CUDA stream.  There is no global mutable state.
+ */
+#ifndef FST_H
+#define FST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FST_ABI_VERSION 1
+#define FST_MAX_SPECIES 16
+
+/* Status codes. */
+enum {
+  FST_OK = 0,
+  FST_ERR_INVALID = -1,     /* bad argument or config                        */
+  FST_ERR_OOM = -2,         /* device or host allocation failed / size limit */
+  FST_ERR_CUDA = -3,        /* a CUDA runtime call failed                    */
+  FST_ERR_TIMEOUT = -4,     /* a bounded device-side wait gave up            */
+  FST_ERR_NONFINITE = -5,   /* a NaN/Inf was found in the state              */
+  FST_ERR_UNSUPPORTED = -6, /* valid FIESTA option this path does not cover  */
+  FST_ERR_SIZE = -7         /* caller buffer size does not match the grid    */
+};
+
+/* Boundary condition types; values match the order of the reference's
+ * `enum class BCType {outflow, reflective, noslip, hydrostatic}`
+ * (src/bc.hpp:31). */
+enum {
+  FST_BC_OUTFLOW = 0,
+  FST_BC_REFLECTIVE = 1,
+  FST_BC_NOSLIP = 2,
+  FST_BC_HYDROSTATIC = 3
+};
+
+/* Arithmetic of the right-hand side. */
+enum {
+  FST_MODE_PLAIN_FP64 = 0, /* the reference's FP64 arithmetic, operation for
+                              operation (bitwise reproducible)              */
+  FST_MODE_MIXED = 1,      /* FP32 reconstruction / fluxes / viscous / C-eq;
+                              FP64 state, EOS recovery and RK combine       */
+  FST_MODE_HYBRID = 2      /* MIXED + learned smoothness classifier routing
+                              smooth faces to the linear upwind flux        */
+};
+
+/*
+ * Run configuration: the fields of the reference's `struct inputConfig`
+ * (src/input.hpp:59-148) that the RHS path reads, filled from the same Lua
+ * deck keys (src/input.cpp:139-308).
+ */
+typedef struct fst_config {
+  int abi_version;           /* must be FST_ABI_VERSION                     */
+  int ndim;                  /* 2 or 3 (fiesta.grid.ndim)                   */
+  int nci, ncj, nck;         /* interior cells (fiesta.grid.ni); nck=1 in 2D */
+  int ng;                    /* ghost layers; must be 3 (fiesta.ng)         */
+  double dx, dy, dz;         /* cell sizes (fiesta.grid.dx); 2D: dz ignored */
+  double dt;                 /* fixed time step (fiesta.time.dt)            */
+  int ns;                    /* number of species (#fiesta.species)         */
+  double R;                  /* universal gas constant (fiesta.R)           */
+  double gamma[FST_MAX_SPECIES]; /* species ratio of specific heats         */
+  double M[FST_MAX_SPECIES];     /* species molar mass                      */
+  double mu[FST_MAX_SPECIES];    /* species dynamic viscosity               */
+  int visc;                  /* fiesta.viscosity.enabled                    */
+  int ceq;                   /* fiesta.ceq.enabled                          */
+  double kap, eps, alpha;    /* fiesta.ceq.kappa / epsilon / alpha          */
+  int buoyancy;              /* fiesta.buoyancy.enabled                     */
+  double g_accel, rho_ref;   /* fiesta.buoyancy.acceleration / rho_reference */
+  int xper, yper, zper;      /* fiesta.bc.{x,y,z}periodic                   */
+  int bc_xmin, bc_xmax, bc_ymin, bc_ymax, bc_zmin, bc_zmax; /* FST_BC_*     */
+  int mode;                  /* FST_MODE_*                                  */
+  int audit_every;           /* HYBRID: full-WENO audit step period (0: never) */
+  int reserved[8];           /* zero                                        */
+} fst_config;
+
+/* Per-context statistics (fst_stats). */
+typedef struct fst_stats {
+  double max_wave_speed;     /* maxS of the last C-equation stage           */
+  double max_chat;           /* maxCh of the last C-equation stage          */
+  double last_step_ms;       /* device time of the last fst_rk_step call    */
+  double flagged_face_fraction; /* HYBRID: WENO share of faces, last stage  */
+  int64_t steps;             /* RK steps taken since creation               */
+  int64_t kernel_launches;   /* kernels launched since creation             */
+  int nonfinite;             /* 1 if the last check found NaN/Inf           */
+  int reserved[7];
+} fst_stats;
+
+typedef struct fst_ctx fst_ctx;
+
+/* Fill `cfg` with defaults (the reference's deck defaults where it has them:
+ * R = 8.314462, ng = 3, outflow BCs, plain FP64). */
+void fst_config_defaults(fst_config* cfg);
+
+/* Size of one state array in doubles: ngi*ngj*ngk*nvt. */
+size_t fst_state_size(const fst_config* cfg);
+
+/* Number of total variables nvt (nv + 5 with the C-equation). */
+int fst_nvt(const fst_config* cfg);
+
+/* Replaces the reference's cart3d_func / cart2d_func constructors
+ * (src/cart3d.cpp:44-174, src/cart2d.cpp:29-134): validates the config,
+ * allocates the device state and work arrays, uploads the species table.
+ * The state starts at zero like a fresh Kokkos View. */
+int fst_create(const fst_config* cfg, fst_ctx** out);
+void fst_destroy(fst_ctx* ctx);
+const char* fst_last_error(const fst_ctx* ctx);
+
+/* Optional: order all work on this cudaStream_t (default: a private stream). */
+int fst_set_stream(fst_ctx* ctx, void* cuda_stream);
+int fst_synchronize(fst_ctx* ctx);
+
+/* State transfer from / to host memory, LayoutLeft, n = fst_state_size().
+ * Replaces the deep_copy of loadInitialConditions (src/input.cpp:515) and
+ * the restart reader / writer's state access. */
+int fst_set_state(fst_ctx* ctx, const double* U, size_t n);
+int fst_get_state(fst_ctx* ctx, double* U, size_t n);
+
+/* Same, from / to device memory on the context's GPU (no host staging). */
+int fst_set_state_device(fst_ctx* ctx, const double* d_U, size_t n);
+int fst_get_state_device(fst_ctx* ctx, double* d_U, size_t n);
+
+/* Ghost fill of the current state: replaces applyBCs (src/bc.cpp:179-249)
+ * with periodic self-copies in the order x, y, z (src/bc.cpp:202-214) and
+ * then the face fills x-, x+, y-, y+, z-, z+ (src/bc.cpp:217-247). */
+int fst_apply_bcs(fst_ctx* ctx);
+
+/* One right-hand-side evaluation of the current state: replaces
+ * cart3d_func::compute (src/cart3d.cpp:220-298, which applies BCs first) and
+ * cart2d_func::compute (src/cart2d.cpp:151-237, which does not).  If R is not
+ * NULL the RHS `dvar` (LayoutLeft, zero outside the interior) is copied to it.
+ * n = fst_state_size(). */
+int fst_compute_rhs(fst_ctx* ctx, double* R, size_t n);
+
+/* `nsteps` time steps: each is preStep (2D: applyBCs, src/cart2d.cpp:147-149)
+ * followed by rkAdvance (src/rk.cpp:28-70): two RHS evaluations and the two
+ * stage combines. */
+int fst_rk_step(fst_ctx* ctx, int nsteps);
+
+/* Secondary variables of the current state over all cells, replacing
+ * calculateRhoPT + computeVelocity + copyExtraVars (src/secondary.hpp:25-151):
+ * 3D: u, v, w, p, T, rho (6 fields); 2D: u, v, p, T, rho (5 fields), each
+ * LayoutLeft (ngi, ngj, ngk, nfields).  n = ngi*ngj*ngk*nfields. */
+int fst_secondary(fst_ctx* ctx, double* varx, size_t n);
+
+/* Scan the state for NaN/Inf (sets stats.nonfinite); FST_ERR_NONFINITE if any. */
+int fst_check_finite(fst_ctx* ctx);
+
+int fst_get_stats(const fst_ctx* ctx, fst_stats* out);
+
+/* Seeded initial conditions generated on the host (same on every platform;
+ * no libm calls).  `kind`: FST_IC_*.  Writes the interior of U (LayoutLeft,
+ * n = fst_state_size()); ghosts and C variables are set to zero. */
+enum {
+  FST_IC_SHOCK_TUBE_2D = 1,   /* Sod tube, diaphragm at x = 0.5            */
+  FST_IC_EXPANSION_3D = 2,    /* high-pressure sphere of species 2 + noise */
+  FST_IC_MIXING_3D = 3,       /* Gaussian pressure kernels + species blobs */
+  FST_IC_RT_2D = 4,           /* Rayleigh-Taylor interface, Fourier modes  */
+  FST_IC_RANDOM_SMOOTH = 5    /* smooth random fields (tests)              */
+};
+typedef struct fst_ic_params {
+  int kind;
+  uint64_t seed;
+  double p_ambient, T_ambient;   /* Pa, K                                    */
+  double p_high;                 /* expansion: bubble pressure             */
+  double radius;                 /* expansion: bubble radius               */
+  double noise;                  /* relative density noise amplitude       */
+  double rho_heavy, rho_light;   /* RT                                     */
+  int nkernels;                  /* mixing: number of pressure kernels     */
+  int reserved[7];
+} fst_ic_params;
+int fst_fill_initial_conditions(const fst_config* cfg, const fst_ic_params* ic,
+                                double* U, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FST_H */
