@@ -1,0 +1,344 @@
+"""Benchmark: Mcell-steps/s of the FIESTA RK2 step (RHS + update) on the
+3D five-species viscous mixing case at 256^3 (C-equation on), one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--modes plain,mixed,hybrid] [--size 256]
+
+A step is one time step of rkAdvance (src/rk.cpp:28-70): two RHS
+evaluations, two stage combines and the ghost fills.  Inputs are synthetic
+(the seeded compiled IC generator; the reference publishes no dataset), the
+state (2 GB at 256^3) is far larger than L2, and dt is fixed from the initial
+state as 0.5*dx/max(|u|+c).
+
+Prints one JSON line.  `value` is the device-timed throughput with the state
+resident in HBM; `e2e` is the same step driven through the C ABI with host
+buffers (state uploaded from pinned memory and downloaded every step).
+`--impl reference` times the reference's algorithm on the host cores instead
+(the compiled reference sources where they were built, else the CPU oracle
+restatement) and prints the same line with "impl": "reference".
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s 256^3 5-species viscous RK2 (FP64 plain / mixed / hybrid)"
+WORKLOAD = "3D five-species viscous mixing, C-equation on, 256^3 interior, outflow BCs"
+SPECIES = [dict(gamma=g, M=m / 1000.0, mu=mu) for g, m, mu in
+           zip([1.4, 1.67, 1.3, 1.32, 1.4], [28.96, 4.0, 44.0, 16.0, 2.0],
+               [1.8e-5, 1.99e-5, 1.47e-5, 1.1e-5, 0.88e-5])]
+SEED = 20261206
+IC_KW = dict(p_ambient=1e5, T_ambient=300.0, nkernels=8)
+MODES = {"plain": 0, "mixed": 1, "hybrid": 2}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def make_cfg(n, mode, dt=1.0):
+    from fiesta_gb300 import abi
+    return abi.make_config(3, (n, n, n), dt=dt, species=SPECIES, visc=True, ceq=True, kap=10.0,
+                           eps=0.4, alpha=40.0, mode=mode)
+
+
+def max_wave_speed(cfg, U):
+    """max(|u| + c) over the interior, with the mixture gamma of the EOS."""
+    ng = cfg.ng
+    I = U[ng:-ng, ng:-ng, ng:-ng]
+    rho = sum(I[..., 4 + s] for s in range(cfg.ns))
+    Cp = sum(I[..., 4 + s] / rho * (cfg.gamma[s] * cfg.R / cfg.M[s] / (cfg.gamma[s] - 1))
+             for s in range(cfg.ns))
+    Cv = sum(I[..., 4 + s] / rho * (cfg.R / cfg.M[s] / (cfg.gamma[s] - 1)) for s in range(cfg.ns))
+    gam = Cp / Cv
+    ke = 0.5 * (I[..., 0] ** 2 + I[..., 1] ** 2 + I[..., 2] ** 2) / rho
+    p = (gam - 1) * (I[..., 3] - ke)
+    c = np.sqrt(gam * p / rho)
+    u = np.sqrt(I[..., 0] ** 2 + I[..., 1] ** 2 + I[..., 2] ** 2) / rho
+    return float((u + c).max())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, flag in zip(names, parts[4:8]):
+                if flag.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# Algorithmic bytes per launch of each plain-path kernel (FP64 = 8 B): the
+# fields it must read and write once, counted over the cells it covers.
+def algorithmic_bytes(kernel, cfg):
+    nci, ncj, nck, ns = cfg.nci, cfg.ncj, cfg.nck, cfg.ns
+    nv = 4 + ns
+    nvt = nv + 5
+    ngi, ngj, ngk = nci + 6, ncj + 6, nck + 6
+    allc = ngi * ngj * ngk
+    faces = (nci + 1) * (ncj + 1) * (nck + 1)
+    inner = nci * ncj * nck
+    tab = {
+        "prim3d": allc * (nv + 1 + 5 + ns + 1),
+        "flux3d": faces * (nv + 4 + 3 * nv),
+        "faces3d": faces * (3 + ns + 1 + 4 + 18 + 27),
+        "cell3d": inner * (3 * nv + 6 + 18 + 27 + 5 + 2 * nvt),
+    }
+    return 8 * tab[kernel] if kernel in tab else None
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_256cubed.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_steps):
+    import torch
+    from fiesta_gb300 import abi
+    from fiesta_gb300.solver import Solver, lib
+    cfg = make_cfg(n, MODES[mode_name], dt)
+    s = Solver(cfg)
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream.cuda_stream)
+    s.set_state(U0)
+    for _ in range(warmup):
+        s.rk_step(1)
+    torch.cuda.synchronize()
+    l0 = s.stats()["kernel_launches"]
+    s.set_profiling(True)
+    s.kernel_times()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler() as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(steps):
+            s.rk_step(1)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    kt = s.kernel_times()
+    s.set_profiling(False)
+    launches = s.stats()["kernel_launches"] - l0
+    cells = cfg.nci * cfg.ncj * cfg.nck
+    value = cells * steps / (ms / 1e3) / 1e6
+    finite = s.check_finite()
+
+    # dominant kernel and its live roofline
+    top = max(kt.items(), key=lambda kv: kv[1][1]) if kt else None
+    roof = None
+    if top:
+        name, (nl, tot) = top
+        per_ms = tot / nl
+        b = algorithmic_bytes(name, cfg)
+        ach = b / (per_ms / 1e3) / 1e9 if b else None
+        roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak_gbs, "unit": "GB/s",
+                "frac": ach / peak_gbs if ach else None, "traffic": read_traffic(name),
+                "algorithmic_bytes_per_launch": b, "avg_launch_ms": per_ms,
+                "peak_source": peak_kind,
+                "share_of_step": tot / ms}
+
+    # end to end through the C ABI with host buffers: upload, step, download
+    n_state = int(np.prod(abi.dims(cfg)))
+    host = torch.empty(n_state, dtype=torch.float64, pin_memory=True)
+    host.numpy()[:] = np.asfortranarray(U0).ravel(order="F")
+    L = lib()
+    ptr = C.cast(C.c_void_p(host.data_ptr()), C.POINTER(C.c_double))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        assert L.fst_set_state(s._ctx, ptr, n_state) == 0
+        assert L.fst_rk_step(s._ctx, 1) == 0
+        assert L.fst_get_state(s._ctx, ptr, n_state) == 0
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_val = cells * e2e_steps / (max(e2e_ms / 1e3, wall)) / 1e6
+    s.close()
+    return {
+        "value": value, "ms_per_step": ms / steps, "gpu_launches": launches,
+        "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
+        "roofline": roof, "clocks": clk.summary(), "finite": finite,
+        "e2e": {"value": e2e_val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": n_state * 8,
+                "d2h_bytes_per_step": n_state * 8, "steps": e2e_steps},
+    }
+
+
+def cpu_sample(n_sample=128, steps=1):
+    """The CPU oracle (restatement of the reference's FP64 path) on a bounded
+    sample of the same workload, all host threads."""
+    from fiesta_gb300 import abi
+    from fiesta_gb300.solver import initial_conditions
+    from oracle.oracle import Oracle
+    cores = os.cpu_count() or 1
+    Oracle.set_threads(cores)
+    cfg = make_cfg(n_sample, 0, 1.0)
+    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, SEED, **IC_KW)
+    cfg.dt = 0.5 * cfg.dx / max_wave_speed(cfg, U0)
+    o = Oracle(cfg)
+    o.set_state(U0)
+    t0 = time.perf_counter()
+    o.rk_step(steps)
+    dt = time.perf_counter() - t0
+    val = n_sample ** 3 * steps / dt / 1e6
+    return {"value": val, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} step(s) of the same case at {n_sample}^3 "
+                      f"(CPU oracle, OpenMP, {cores} threads, {dt:.1f} s)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--modes", default="plain")
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    a.warmup = max(a.warmup, 3)
+
+    if a.impl == "reference":
+        # The reference has no GPU path of its own here (Kokkos is not
+        # installable); its algorithm is timed on the host cores.
+        if rank != 0:
+            return
+        t0 = time.perf_counter()
+        runs = [cpu_sample(a.cpu_sample, 1) for _ in range(max(1, min(a.steps, 3)))]
+        val = statistics.median(r["value"] for r in runs)
+        cb = dict(runs[0])
+        cb["value"] = val
+        cb["sample"] += f"; median of {len(runs)} runs"
+        line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "Mcell-steps/s",
+                "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+                "ms_per_step": (a.cpu_sample ** 3) / (val * 1e6) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": WORKLOAD, "grid": [a.size] * 3,
+                                                "species": 5, "sample_grid": [a.cpu_sample] * 3},
+                "cpu_baseline": cb,
+                "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "wall_s": time.perf_counter() - t0}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from fiesta_gb300 import abi
+    from fiesta_gb300.solver import initial_conditions
+    if world > 1:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    peak, peak_kind = load_peaks()
+    n = a.size
+    cfg0 = make_cfg(n, 0, 1.0)
+    U0 = initial_conditions(cfg0, abi.IC_MIXING_3D, SEED, **IC_KW)
+    S0 = max_wave_speed(cfg0, U0)
+    dt = 0.5 * cfg0.dx / S0
+    modes = [m.strip() for m in a.modes.split(",") if m.strip()]
+    results = {}
+    for m in modes:
+        results[m] = run_gpu_mode(m, n, a.steps, a.warmup, U0, dt, peak, peak_kind, a.e2e_steps)
+    # replicas only: each rank runs the whole case; whole-job value sums ranks
+    head = modes[-1]
+    r = results[head]
+    value, ms = r["value"], r["ms_per_step"]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        value = world * (n ** 3) / (ms / 1e3) / 1e6
+    if rank != 0:
+        return
+    cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if head == "plain" else "f32+f64",
+        "data": "synthetic (seeded compiled IC generator: 8 Gaussian pressure kernels, 5 species)",
+        "config": {"workload": WORKLOAD, "grid": [n] * 3, "species": 5, "nvt": 14,
+                   "mode": head, "dt": dt, "l2": "state 2.0 GB > L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": r["roofline"], "cpu_baseline": cpu, "clocks": r["clocks"],
+        "e2e": r["e2e"], "gpu_launches": r["gpu_launches"],
+        "modes": {m: {k: v for k, v in results[m].items() if k not in ("clocks",)} for m in modes},
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -78,6 +78,10 @@ class FstStats(C.Structure):
     ]
 
 
+class FstKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_int64), ("total_ms", C.c_double)]
+
+
 class FstIcParams(C.Structure):
     _fields_ = [
         ("kind", C.c_int),

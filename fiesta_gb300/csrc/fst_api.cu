@@ -1,0 +1,543 @@
+// fst_api.cu — the libfst C ABI (include/fst.h): context lifetime, state
+// transfer, and the per-step sequencing that replaces rkAdvance
+// (src/rk.cpp:28-70) with its calls into cart3d_func / cart2d_func::compute.
+//
+// State lives in two device buffers A and B.  Stage 1 reads A, writes
+// B = A + (0.5*dt)*R(A); stage 2 reads B and writes A = A + dt*R(B) in place
+// (each cell reads only its own old value).  This replaces the reference's
+// tmp1 copy and its separate dvar array: the stage combine is fused into the
+// cell kernel and R never goes to HBM.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fst_common.cuh"
+#include "fst_internal.h"
+
+namespace {
+
+DivC make_div(double d) {
+  DivC q;
+  q.d = d;
+  int e = 0;
+  double m = std::frexp(d, &e);
+  q.inv = (d > 0.0 && m == 0.5 && std::isfinite(1.0 / d)) ? 1.0 / d : 0.0;
+  return q;
+}
+
+bool bc_ok(int t) { return t >= FST_BC_OUTFLOW && t <= FST_BC_HYDROSTATIC; }
+
+}  // namespace
+
+struct fst_ctx {
+  fst_config cf;
+  Geo g;
+  Phys P;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  double* Ua = nullptr;
+  double* Ub = nullptr;
+  double* Rdev = nullptr;  // compute_rhs output (zero outside the interior)
+  Plain3DBufs b3{};
+  Plain2DBufs b2{};
+  MixedBufs bm{};
+  std::vector<void*> allocs;
+  std::vector<size_t> alloc_bytes;
+  std::string err;
+  fst_stats stats{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timed = false;
+  int* dflag = nullptr;
+  Prof prof;
+};
+
+namespace {
+
+int fail(fst_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(fst_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, FST_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int check_launch(fst_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  return FST_OK;
+}
+
+// Reads FST_MAX_DEVICE_BYTES: an artificial device-memory limit used to
+// exercise the out-of-memory path without exhausting a GPU.
+size_t device_limit() {
+  const char* s = std::getenv("FST_MAX_DEVICE_BYTES");
+  if (!s || !*s) return (size_t)-1;
+  return (size_t)std::strtoull(s, nullptr, 10);
+}
+
+std::string validate(const fst_config* cf) {
+  if (cf->abi_version != FST_ABI_VERSION) return "abi_version mismatch";
+  if (cf->ndim != 2 && cf->ndim != 3) return "ndim must be 2 or 3";
+  if (cf->ng != 3) return "ng must be 3 (the WENO5 stencil needs three ghost layers)";
+  if (cf->nci < 1 || cf->ncj < 1 || (cf->ndim == 3 && cf->nck < 1)) return "grid sizes must be >= 1";
+  if (cf->ns < 1 || cf->ns > FST_MAX_SPECIES) return "ns must be in [1, 16]";
+  if (!(cf->dx > 0) || !(cf->dy > 0) || (cf->ndim == 3 && !(cf->dz > 0)))
+    return "cell sizes must be positive";
+  if (!std::isfinite(cf->dt)) return "dt must be finite";
+  for (int s = 0; s < cf->ns; ++s) {
+    if (!(cf->gamma[s] > 1.0)) return "species gamma must be > 1";
+    if (!(cf->M[s] > 0.0)) return "species molar mass must be > 0";
+  }
+  const int b[6] = {cf->bc_xmin, cf->bc_xmax, cf->bc_ymin, cf->bc_ymax, cf->bc_zmin, cf->bc_zmax};
+  for (int q = 0; q < 6; ++q)
+    if (!bc_ok(b[q])) return "unknown boundary condition type";
+  if (cf->mode < FST_MODE_PLAIN_FP64 || cf->mode > FST_MODE_HYBRID) return "unknown mode";
+  long long ngi = cf->nci + 6LL, ngj = cf->ncj + 6LL, ngk = cf->ndim == 3 ? cf->nck + 6LL : 1;
+  if (ngi * ngj * ngk > (1LL << 40)) return "grid too large";
+  return "";
+}
+
+void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
+  std::memset(&P, 0, sizeof(P));
+  P.ns = g.ns;
+  P.nv = g.nv;
+  P.nvt = g.nvt;
+  P.visc = cf.visc != 0;
+  P.ceq = cf.ceq != 0;
+  P.buoyancy = cf.buoyancy != 0;
+  // device config array of the reference (src/cart3d.cpp:152-171)
+  std::vector<double> cd(6 + 3 * g.ns, 0.0);
+  for (int s = 0; s < g.ns; ++s) {
+    cd[6 + 3 * s] = cf.gamma[s];
+    cd[7 + 3 * s] = cf.R / cf.M[s];
+    cd[8 + 3 * s] = cf.mu[s];
+  }
+  for (int s = 0; s < g.ns; ++s) {
+    double gs = cd[6 + 3 * s], Rs = cd[7 + 3 * s];
+    P.cp_s[s] = gs * Rs / (gs - 1);
+    P.cv_s[s] = Rs / (gs - 1);
+    P.mu_s[s] = cd[8 + 3 * s];
+    double g2 = cd[6 + 2 * s], R2 = cd[6 + 2 * s + 1];
+    P.cp2_s[s] = g2 * R2 / (g2 - 1);
+    P.cv2_s[s] = R2 / (g2 - 1);
+  }
+  P.dx = cf.dx;
+  P.dy = cf.dy;
+  P.dz = g.ndim == 3 ? cf.dz : cf.dx;  // 2D: dz = dx (src/input.cpp:402)
+  P.ddx = make_div(P.dx);
+  P.ddy = make_div(P.dy);
+  P.ddz = make_div(P.dz);
+  P.d4x = make_div(4 * P.dx);
+  P.d4y = make_div(4 * P.dy);
+  P.d4z = make_div(4 * P.dz);
+  P.d12x = 12.0 * P.dx;
+  P.d12y = 12.0 * P.dy;
+  P.d12z = 12.0 * P.dz;
+  P.d12pz = 12.0 * P.dy;
+  P.dt = cf.dt;
+  P.hdt = 0.5f * cf.dt;
+  P.kap = cf.kap;
+  P.eps = cf.eps;
+  P.alpha = cf.alpha;
+  P.g = cf.g_accel;
+  P.rho_ref = cf.rho_ref;
+  if (g.ndim == 3) {
+    P.dxmag2 = P.dx * P.dx + P.dy * P.dy + P.dz * P.dz;
+    P.dxmag = std::sqrt(P.dx * P.dx + P.dy * P.dy + P.dz * P.dz);
+  } else {
+    P.dxmag2 = P.dx * P.dx + P.dy * P.dy;
+    P.dxmag = std::sqrt(P.dx * P.dx + P.dy * P.dy);
+  }
+  P.mu2d = 2.928e-5;
+  P.kheat2d = 0.026;
+}
+
+// Device bytes of the work arrays of each path, in doubles per cell.
+size_t work_doubles_per_cell(const fst_config& cf, const Geo& g) {
+  size_t w = 0;
+  if (cf.mode == FST_MODE_PLAIN_FP64) {
+    if (g.ndim == 3) {
+      w = 2 + 3 + 1 + 1 + (size_t)3 * g.nv;  // rho p vel T nrg F
+      if (cf.visc) w += g.ns + 18;
+      if (cf.ceq) w += 27;
+    } else {
+      w = 2 + 2 + 1 + 1 + (size_t)2 * g.nv;
+      if (cf.visc) w += 6 + 2;
+      if (cf.ceq) w += 8;
+    }
+  } else {
+    w = fst_mixed_work_doubles_per_cell(cf, g);
+  }
+  return w;
+}
+
+__global__ void k_nonfinite(const double* __restrict__ U, long long n, int* flag) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; t < n; t += (long long)gridDim.x * blockDim.x)
+    if (!isfinite(U[t])) {
+      *flag = 1;
+      return;
+    }
+}
+
+int alloc(fst_ctx* c, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, FST_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  c->allocs.push_back(*p);
+  c->alloc_bytes.push_back(bytes);
+  return FST_OK;
+}
+
+template <class T>
+int allocd(fst_ctx* c, T** p, size_t n) {
+  return alloc(c, (void**)p, n * sizeof(T));
+}
+
+int stage(fst_ctx* c, const double* Uin, const double* Uold, double* Unew, double coef,
+          double* Rout, bool ghosts) {
+  int n;
+  if (c->cf.mode != FST_MODE_PLAIN_FP64)
+    n = fst_mixed_stage(c->g, c->P, c->cf, c->bm, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
+                        &c->prof);
+  else if (c->g.ndim == 3)
+    n = fst_plain3d_stage(c->g, c->P, c->b3, Uin, Uold, Unew, coef, Rout, c->stream, &c->prof);
+  else
+    n = fst_plain2d_stage(c->g, c->P, c->b2, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
+                          &c->prof);
+  c->stats.kernel_launches += n;
+  return check_launch(c, "stage kernels");
+}
+
+int bcs(fst_ctx* c, double* U) {
+  c->stats.kernel_launches += fst_launch_bcs(c->g, c->cf, U, c->stream, &c->prof);
+  return check_launch(c, "boundary kernels");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fst_last_error(const fst_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int fst_create(const fst_config* cfg, fst_ctx** out) {
+  if (!cfg || !out) return FST_ERR_INVALID;
+  *out = nullptr;
+  std::string why = validate(cfg);
+  if (!why.empty()) {
+    std::fprintf(stderr, "fst_create: %s\n", why.c_str());
+    return FST_ERR_INVALID;
+  }
+  fst_ctx* c = new fst_ctx();
+  c->cf = *cfg;
+  Geo& g = c->g;
+  g.ndim = cfg->ndim;
+  g.ng = cfg->ng;
+  g.nci = cfg->nci;
+  g.ncj = cfg->ncj;
+  g.nck = g.ndim == 3 ? cfg->nck : 1;
+  g.ngi = g.nci + 2 * g.ng;
+  g.ngj = g.ncj + 2 * g.ng;
+  g.ngk = g.ndim == 3 ? g.nck + 2 * g.ng : 1;
+  g.ns = cfg->ns;
+  g.nv = (g.ndim == 3 ? 4 : 3) + g.ns;
+  g.nvt = g.nv + (cfg->ceq ? 5 : 0);
+  g.sy = g.ngi;
+  g.sz = (long long)g.ngi * g.ngj;
+  g.sv = g.sz * g.ngk;
+  setup_phys(*cfg, g, c->P);
+
+  const size_t cells = (size_t)g.sv;
+  const size_t need = cells * sizeof(double) * (2 * (size_t)g.nvt + work_doubles_per_cell(*cfg, g));
+  if (need > device_limit()) {
+    std::fprintf(stderr, "fst_create: %zu device bytes over the FST_MAX_DEVICE_BYTES limit\n", need);
+    delete c;
+    return FST_ERR_OOM;
+  }
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "fst_create: no CUDA device: %s\n", cudaGetErrorString(e));
+    cudaGetLastError();
+    delete c;
+    return FST_ERR_CUDA;
+  }
+  int rc = FST_OK;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaStreamCreate");
+  c->own_stream = true;
+  const size_t nst = cells * g.nvt;
+  if (!rc) rc = allocd(c, &c->Ua, nst);
+  if (!rc) rc = allocd(c, &c->Ub, nst);
+  if (!rc) rc = allocd(c, &c->dflag, 1);
+  if (!rc && cfg->mode == FST_MODE_PLAIN_FP64 && g.ndim == 3) {
+    Plain3DBufs& b = c->b3;
+    rc = allocd(c, &b.rho, cells);
+    if (!rc) rc = allocd(c, &b.pr, cells);
+    if (!rc) rc = allocd(c, &b.vel, 3 * cells);
+    if (!rc) rc = allocd(c, &b.T, cells);
+    if (!rc) rc = allocd(c, &b.nrg, cells);
+    if (!rc) rc = allocd(c, &b.F, (size_t)3 * g.nv * cells);
+    if (!rc && cfg->visc) rc = allocd(c, &b.Y, (size_t)g.ns * cells);
+    if (!rc && cfg->visc) rc = allocd(c, &b.S, 18 * cells);
+    if (!rc && cfg->ceq) rc = allocd(c, &b.MF, 27 * cells);
+    if (!rc) rc = allocd(c, &b.red, 2);
+  } else if (!rc && cfg->mode == FST_MODE_PLAIN_FP64) {
+    Plain2DBufs& b = c->b2;
+    rc = allocd(c, &b.rho, cells);
+    if (!rc) rc = allocd(c, &b.pr, cells);
+    if (!rc) rc = allocd(c, &b.vel, 2 * cells);
+    if (!rc) rc = allocd(c, &b.T, cells);
+    if (!rc) rc = allocd(c, &b.nrg, cells);
+    if (!rc) rc = allocd(c, &b.F, (size_t)2 * g.nv * cells);
+    if (!rc && cfg->visc) rc = allocd(c, &b.S, 6 * cells);
+    if (!rc && cfg->visc) rc = allocd(c, &b.Q, 2 * cells);
+    if (!rc && cfg->ceq) rc = allocd(c, &b.MF, 8 * cells);
+    if (!rc) rc = allocd(c, &b.red, 2);
+  } else if (!rc) {
+    rc = fst_mixed_alloc(*cfg, g, c->bm, [&](void** p, size_t bytes) { return alloc(c, p, bytes); });
+  }
+  // zero state like a fresh Kokkos View; zero work arrays so that entries
+  // outside each kernel's range read as the reference's zero-initialised ones
+  if (!rc) {
+    for (size_t q = 0; q < c->alloc_bytes.size() && e == cudaSuccess; ++q)
+      e = cudaMemsetAsync(c->allocs[q], 0, c->alloc_bytes[q], c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaMemset");
+  }
+  if (!rc) {
+    e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaEventCreate");
+  }
+  if (!rc) {
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "create sync");
+  }
+  if (rc) {
+    std::fprintf(stderr, "fst_create: %s\n", c->err.c_str());
+    fst_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return FST_OK;
+}
+
+void fst_destroy(fst_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->Rdev) cudaFree(c->Rdev);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int fst_set_stream(fst_ctx* c, void* s) {
+  if (!c) return FST_ERR_INVALID;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "set_stream sync");
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->own_stream = false;
+  c->stream = (cudaStream_t)s;
+  return FST_OK;
+}
+
+int fst_synchronize(fst_ctx* c) {
+  if (!c) return FST_ERR_INVALID;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "synchronize");
+  return FST_OK;
+}
+
+int fst_set_state(fst_ctx* c, const double* U, size_t n) {
+  if (!c || !U) return FST_ERR_INVALID;
+  if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  cudaError_t e = cudaMemcpyAsync(c->Ua, U, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "set_state");
+  return FST_OK;
+}
+
+int fst_get_state(fst_ctx* c, double* U, size_t n) {
+  if (!c || !U) return FST_ERR_INVALID;
+  if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  cudaError_t e = cudaMemcpyAsync(U, c->Ua, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "get_state");
+  return FST_OK;
+}
+
+int fst_set_state_device(fst_ctx* c, const double* dU, size_t n) {
+  if (!c || !dU) return FST_ERR_INVALID;
+  if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  cudaError_t e = cudaMemcpyAsync(c->Ua, dU, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "set_state_device");
+  return FST_OK;
+}
+
+int fst_get_state_device(fst_ctx* c, double* dU, size_t n) {
+  if (!c || !dU) return FST_ERR_INVALID;
+  if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  cudaError_t e = cudaMemcpyAsync(dU, c->Ua, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "get_state_device");
+  return FST_OK;
+}
+
+int fst_apply_bcs(fst_ctx* c) {
+  if (!c) return FST_ERR_INVALID;
+  return bcs(c, c->Ua);
+}
+
+int fst_compute_rhs(fst_ctx* c, double* R, size_t n) {
+  if (!c) return FST_ERR_INVALID;
+  const size_t nst = (size_t)c->g.sv * c->g.nvt;
+  if (R && n != nst) return fail(c, FST_ERR_SIZE, "rhs size mismatch");
+  if (!c->Rdev) {
+    cudaError_t e = cudaMalloc(&c->Rdev, nst * sizeof(double));
+    if (e != cudaSuccess) {
+      c->Rdev = nullptr;
+      cudaGetLastError();
+      return fail(c, FST_ERR_OOM, "rhs buffer allocation failed");
+    }
+    e = cudaMemsetAsync(c->Rdev, 0, nst * sizeof(double), c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "rhs memset");
+  }
+  int rc = FST_OK;
+  if (c->g.ndim == 3) rc = bcs(c, c->Ua);  // cart3d_func::compute applies BCs first
+  if (!rc) rc = stage(c, c->Ua, c->Ua, nullptr, 0.0, c->Rdev, false);
+  if (rc) return rc;
+  if (R) {
+    cudaError_t e = cudaMemcpyAsync(R, c->Rdev, nst * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "compute_rhs copy");
+  }
+  return FST_OK;
+}
+
+int fst_rk_step(fst_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return FST_ERR_INVALID;
+  cudaEventRecord(c->ev0, c->stream);
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = FST_OK;
+    const bool two_d = c->g.ndim == 2;
+    if (two_d) rc = bcs(c, c->Ua);  // cart2d_func::preStep
+    if (!rc && !two_d) rc = bcs(c, c->Ua);
+    if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, two_d);
+    if (!rc && !two_d) rc = bcs(c, c->Ub);
+    if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
+    if (rc) return rc;
+    c->stats.steps += 1;
+  }
+  cudaEventRecord(c->ev1, c->stream);
+  c->timed = nsteps > 0;
+  return check_launch(c, "rk_step");
+}
+
+int fst_secondary(fst_ctx* c, double* out, size_t n) {
+  if (!c || !out) return FST_ERR_INVALID;
+  const Geo& g = c->g;
+  const size_t nc = (size_t)g.sv;
+  const int nf = g.ndim == 3 ? 6 : 5;
+  if (n != nc * nf) return fail(c, FST_ERR_SIZE, "secondary size mismatch");
+  const double *rho, *pr, *vel, *T;
+  if (c->cf.mode != FST_MODE_PLAIN_FP64) {
+    c->stats.kernel_launches += fst_mixed_secondary(g, c->P, c->bm, c->Ua, c->stream, &rho, &pr, &vel, &T);
+  } else if (g.ndim == 3) {
+    c->stats.kernel_launches += fst_plain3d_secondary(g, c->P, c->b3, c->Ua, c->stream);
+    rho = c->b3.rho; pr = c->b3.pr; vel = c->b3.vel; T = c->b3.T;
+  } else {
+    c->stats.kernel_launches += fst_plain2d_secondary(g, c->P, c->b2, c->Ua, c->stream);
+    rho = c->b2.rho; pr = c->b2.pr; vel = c->b2.vel; T = c->b2.T;
+  }
+  int rc = check_launch(c, "secondary");
+  if (rc) return rc;
+  const size_t B = nc * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  for (int d = 0; d < g.ndim && e == cudaSuccess; ++d)
+    e = cudaMemcpyAsync(out + nc * d, vel + nc * d, B, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out + nc * g.ndim, pr, B, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out + nc * (g.ndim + 1), T, B, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out + nc * (g.ndim + 2), rho, B, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "secondary copy");
+  return FST_OK;
+}
+
+int fst_check_finite(fst_ctx* c) {
+  if (!c) return FST_ERR_INVALID;
+  const long long n = c->g.sv * c->g.nvt;
+  cudaMemsetAsync(c->dflag, 0, sizeof(int), c->stream);
+  k_nonfinite<<<1216, 256, 0, c->stream>>>(c->Ua, n, c->dflag);
+  c->stats.kernel_launches += 1;
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "check_finite");
+  c->stats.nonfinite = h;
+  return h ? fail(c, FST_ERR_NONFINITE, "non-finite value in state") : FST_OK;
+}
+
+int fst_get_stats(const fst_ctx* cc, fst_stats* out) {
+  if (!cc || !out) return FST_ERR_INVALID;
+  fst_ctx* c = const_cast<fst_ctx*>(cc);
+  cudaStreamSynchronize(c->stream);
+  *out = c->stats;
+  const unsigned long long* red = c->cf.mode != FST_MODE_PLAIN_FP64 ? c->bm.red
+                                  : c->g.ndim == 3 ? c->b3.red : c->b2.red;
+  if (c->cf.ceq && red) {
+    unsigned long long h[2] = {0, 0};
+    if (cudaMemcpy(h, red, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess) {
+      out->max_wave_speed = fst_unkey(h[0]);
+      out->max_chat = fst_unkey(h[1]);
+    }
+  }
+  if (c->timed) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) out->last_step_ms = ms;
+  }
+  out->flagged_face_fraction = fst_mixed_flagged_fraction(c->bm, c->stream);
+  return FST_OK;
+}
+
+int fst_set_profiling(fst_ctx* c, int on) {
+  if (!c) return FST_ERR_INVALID;
+  c->prof.on = on != 0;
+  return FST_OK;
+}
+
+int fst_kernel_times(fst_ctx* c, fst_kernel_time* out, int max, int* count) {
+  if (!c || (!out && max > 0)) return FST_ERR_INVALID;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "kernel_times sync");
+  std::vector<fst_kernel_time> agg;
+  for (auto& r : c->prof.recs) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    size_t q = 0;
+    for (; q < agg.size(); ++q)
+      if (std::strncmp(agg[q].name, r.name, sizeof(agg[q].name)) == 0) break;
+    if (q == agg.size()) {
+      fst_kernel_time t{};
+      std::strncpy(t.name, r.name, sizeof(t.name) - 1);
+      agg.push_back(t);
+    }
+    agg[q].launches += 1;
+    agg[q].total_ms += ms;
+    c->prof.pool.push_back(r.a);
+    c->prof.pool.push_back(r.b);
+  }
+  c->prof.recs.clear();
+  int n = 0;
+  for (; n < (int)agg.size() && n < max; ++n) out[n] = agg[n];
+  if (count) *count = n;
+  return FST_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// fst_common.cuh — shared device-side definitions of libfst.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/fst.h"
+
+#define FST_MAXV (4 + FST_MAX_SPECIES + 5)
+
+// Grid geometry and strides of one field in HBM.  Fields are stored like the
+// reference's CUDA build, LayoutLeft with i fastest:
+//   a[i + sy*j + sz*k + sv*v],  sy = ngi, sz = ngi*ngj, sv = ngi*ngj*ngk.
+struct Geo {
+  int ndim, ng, nci, ncj, nck, ngi, ngj, ngk;
+  int ns, nv, nvt;
+  long long sy, sz, sv;
+};
+
+// Division by a run-time constant d.  When d is a power of two, a/d equals
+// a*(1/d) exactly for every a (both are the correctly rounded a*2^-k), so the
+// multiply is used; otherwise the IEEE division.  Results are bit-identical
+// to a/d either way.
+struct DivC {
+  double d, inv;  // inv = 1/d if d is a power of two, else 0
+  __device__ __forceinline__ double operator()(double a) const {
+    return inv != 0.0 ? a * inv : a / d;
+  }
+};
+
+// Physics constants of one run, passed by value to the kernels.
+struct Phys {
+  int ns, nv, nvt, visc, ceq, buoyancy;
+  // species constants of calculateRhoPT (src/secondary.hpp:127-135):
+  //   cp_s = gammas*Rs/(gammas-1), cv_s = Rs/(gammas-1), Rs = cd(7+3s)
+  double cp_s[FST_MAX_SPECIES], cv_s[FST_MAX_SPECIES], mu_s[FST_MAX_SPECIES];
+  // the same with the stride-2 species table read by maxWaveSpeed2D
+  // (src/ceq.hpp:61-66): gammas = cd(6+2s), Rs = cd(7+2s)
+  double cp2_s[FST_MAX_SPECIES], cv2_s[FST_MAX_SPECIES];
+  double dx, dy, dz;
+  DivC ddx, ddy, ddz;     // x/dx, x/dy, x/dz
+  DivC d4x, d4y, d4z;     // x/(4*dx) ... (viscous and C-equation tangential terms)
+  double d12x, d12y, d12z;  // 12.0*dx, 12.0*dy, 12.0*dz (4th-order derivatives)
+  double d12pz;           // 12.0*cd(2): the reference's dz = cd(2) in presgrad3D
+  double dt, hdt;         // dt and 0.5f*dt
+  double kap, eps, alpha, g, rho_ref;
+  double dxmag2;          // dx^2+dy^2(+dz^2): alpha numerator
+  double dxmag;           // sqrt(dx^2+dy^2(+dz^2)): updateCeq cell size
+  double mu2d;            // constant 2D viscosity 2.928e-5 (src/viscosity.hpp:62-63)
+  double kheat2d;         // 2D heat conductivity 0.026 (src/viscosity.hpp:117)
+};
+
+// --- order-preserving encoding of doubles for atomicMax -------------------
+__device__ __forceinline__ unsigned long long fst_key(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ double fst_unkey(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+#endif
+}
+// Kokkos::Max starts from -DBL_MAX and `if (s > lmax)` never takes a NaN.
+#define FST_KEY_LOWEST 0x0010000000000000ull /* fst_key(-DBL_MAX) */
+
+// Warp-wide max of per-thread maxima that already skipped NaN.
+__device__ __forceinline__ double fst_warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w > v) ? w : v;  // NaN never wins, as in the reference reducer
+  }
+  return v;
+}
+
+// Linear index helpers
+__device__ __forceinline__ long long fst_idx(const Geo& g, int i, int j, int k) {
+  return (long long)i + g.sy * j + g.sz * k;
+}

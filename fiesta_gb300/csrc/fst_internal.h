@@ -1,0 +1,103 @@
+// fst_internal.h — launch entry points shared between the libfst translation
+// units (not part of the public ABI).
+#pragma once
+#include <cstddef>
+#include <functional>
+
+#include <string>
+#include <vector>
+
+#include "fst_common.cuh"
+
+// Optional CUDA-event bracketing of kernel launches (fst_set_profiling).
+struct Prof {
+  bool on = false;
+  struct Rec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t take() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void begin(const char* name, cudaStream_t s) {
+    if (!on) return;
+    Rec r{name, take(), take()};
+    cudaEventRecord(r.a, s);
+    recs.push_back(r);
+  }
+  void end(cudaStream_t s) {
+    if (!on || recs.empty()) return;
+    cudaEventRecord(recs.back().b, s);
+  }
+  ~Prof() {
+    for (auto& r : recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+// Launch with optional event bracketing; counts into `n`.
+#define FST_LAUNCH(prof, name, st, n, ...) \
+  do {                                      \
+    if (prof) (prof)->begin(name, st);      \
+    __VA_ARGS__;                            \
+    if (prof) (prof)->end(st);              \
+    ++(n);                                  \
+  } while (0)
+
+// fst_bc.cu
+int fst_launch_bcs(const Geo& g, const fst_config& cf, double* U, cudaStream_t stream, Prof* prof);
+
+// fst_plain3d.cu
+struct Plain3DBufs {
+  double *rho, *pr, *vel, *Y, *nrg, *T;
+  double *F, *S, *MF;
+  unsigned long long* red;
+};
+int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* Uin,
+                      const double* Uold, double* Unew, double coef, double* Rout,
+                      cudaStream_t st, Prof* prof);
+int fst_plain3d_secondary(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* U,
+                          cudaStream_t st);
+
+// fst_plain2d.cu
+struct Plain2DBufs {
+  double *rho, *pr, *vel, *T, *nrg;
+  double *F, *S, *Q, *MF;
+  unsigned long long* red;
+};
+int fst_plain2d_stage(const Geo& g, const Phys& P, const Plain2DBufs& b, const double* Uin,
+                      const double* Uold, double* Unew, double coef, double* Rout, bool ghosts,
+                      cudaStream_t st, Prof* prof);
+int fst_plain2d_secondary(const Geo& g, const Phys& P, const Plain2DBufs& b, const double* U,
+                          cudaStream_t st);
+
+// fst_mixed.cu (FST_MODE_MIXED / FST_MODE_HYBRID)
+struct MixedBufs {
+  double *rho, *pr, *vel, *T;
+  void* work;          // path-specific work arrays
+  size_t work_bytes;
+  unsigned long long* red;
+  unsigned long long* counters;  // hybrid: [0] faces, [1] WENO faces
+};
+using fst_alloc_fn = std::function<int(void**, size_t)>;
+size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);
+int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc);
+int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
+                    const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
+                    bool ghosts, cudaStream_t st, Prof* prof);
+int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const double* U,
+                        cudaStream_t st, const double** rho, const double** pr, const double** vel,
+                        const double** T);
+double fst_mixed_flagged_fraction(const MixedBufs& b, cudaStream_t st);

@@ -1,0 +1,249 @@
+"""Python binding of libfst (include/fst.h) and a host-side mirror of the
+reference's module interface.
+
+``Solver`` wraps one ``fst_ctx``.  ``Cart3D`` / ``Cart2D`` keep the method
+names and call order of the reference's ``rk_func`` subclasses
+(src/rkfunction.hpp:36-69, src/cart3d.cpp, src/cart2d.cpp) so that driver
+code written against them reads the same:
+
+    f = Cart3D(cfg)            # cart3d_func(cf)
+    f.var = U0                 # loadInitialConditions
+    f.preSim()
+    for t in range(tstart, tend + 1):   # src/main.cpp:61, inclusive
+        f.preStep(); rkAdvance(cfg, f); f.postStep()
+
+There is no CPU fallback: if libfst.so is missing or no GPU is present the
+constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .build import LIB, build, up_to_date
+
+_lib = None
+
+_EXPORTS = {
+    # name: (restype, argtypes)
+    "fst_config_defaults": (None, [C.POINTER(abi.FstConfig)]),
+    "fst_state_size": (C.c_size_t, [C.POINTER(abi.FstConfig)]),
+    "fst_nvt": (C.c_int, [C.POINTER(abi.FstConfig)]),
+    "fst_create": (C.c_int, [C.POINTER(abi.FstConfig), C.POINTER(C.c_void_p)]),
+    "fst_destroy": (None, [C.c_void_p]),
+    "fst_last_error": (C.c_char_p, [C.c_void_p]),
+    "fst_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fst_synchronize": (C.c_int, [C.c_void_p]),
+    "fst_set_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
+    "fst_get_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
+    "fst_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "fst_get_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "fst_apply_bcs": (C.c_int, [C.c_void_p]),
+    "fst_compute_rhs": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
+    "fst_rk_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "fst_secondary": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
+    "fst_check_finite": (C.c_int, [C.c_void_p]),
+    "fst_get_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.FstStats)]),
+    "fst_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "fst_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(abi.FstKernelTime), C.c_int,
+                                   C.POINTER(C.c_int)]),
+    "fst_fill_initial_conditions": (C.c_int, [C.POINTER(abi.FstConfig), C.POINTER(abi.FstIcParams),
+                                              C.POINTER(C.c_double), C.c_size_t]),
+}
+
+
+def lib():
+    """Load fiesta_gb300/libfst.so (building it first if sources are newer)."""
+    global _lib
+    if _lib is None:
+        if not up_to_date():
+            build()
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"libfst.so not found at {LIB}; run __graft_entry__.build()")
+        L = C.CDLL(LIB)
+        for name, (res, args) in _EXPORTS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class FstError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libfst error {code}: {msg}")
+        self.code = code
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def initial_conditions(cfg, kind, seed=0, **kw):
+    """Seeded initial state (fst_fill_initial_conditions), LayoutLeft array."""
+    ic = abi.FstIcParams()
+    ic.kind = kind
+    ic.seed = seed
+    for k, v in kw.items():
+        setattr(ic, k, v)
+    shape = abi.dims(cfg)
+    U = np.zeros(shape, dtype=np.float64, order="F")
+    rc = lib().fst_fill_initial_conditions(C.byref(cfg), C.byref(ic), _dptr(U), U.size)
+    if rc != 0:
+        raise FstError(rc, "fst_fill_initial_conditions")
+    return U
+
+
+class Solver:
+    """One libfst context on the current CUDA device."""
+
+    def __init__(self, cfg):
+        L = lib()
+        self.cfg = cfg
+        self.shape = abi.dims(cfg)
+        self.n = int(np.prod(self.shape))
+        self._ctx = C.c_void_p()
+        rc = L.fst_create(C.byref(cfg), C.byref(self._ctx))
+        if rc != 0:
+            raise FstError(rc, "fst_create failed (see stderr)")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib().fst_last_error(self._ctx)
+            raise FstError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if self._ctx:
+            lib().fst_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ---------------------------------------------------------
+    def set_state(self, U):
+        U = np.asfortranarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"state shape {U.shape} != {self.shape}")
+        self._check(lib().fst_set_state(self._ctx, _dptr(U), self.n), "set_state")
+
+    def get_state(self):
+        U = np.zeros(self.shape, dtype=np.float64, order="F")
+        self._check(lib().fst_get_state(self._ctx, _dptr(U), self.n), "get_state")
+        return U
+
+    def set_state_device(self, ptr):
+        self._check(lib().fst_set_state_device(self._ctx, C.c_void_p(ptr), self.n), "set_state_device")
+
+    def get_state_device(self, ptr):
+        self._check(lib().fst_get_state_device(self._ctx, C.c_void_p(ptr), self.n), "get_state_device")
+
+    # -- the path ------------------------------------------------------
+    def apply_bcs(self):
+        self._check(lib().fst_apply_bcs(self._ctx), "apply_bcs")
+
+    def compute_rhs(self, out=True):
+        if not out:
+            self._check(lib().fst_compute_rhs(self._ctx, None, 0), "compute_rhs")
+            return None
+        R = np.zeros(self.shape, dtype=np.float64, order="F")
+        self._check(lib().fst_compute_rhs(self._ctx, _dptr(R), self.n), "compute_rhs")
+        return R
+
+    def rk_step(self, nsteps=1):
+        self._check(lib().fst_rk_step(self._ctx, int(nsteps)), "rk_step")
+
+    def secondary(self):
+        nf = 6 if self.cfg.ndim == 3 else 5
+        out = np.zeros(self.shape[:3] + (nf,), dtype=np.float64, order="F")
+        self._check(lib().fst_secondary(self._ctx, _dptr(out), out.size), "secondary")
+        return out
+
+    def check_finite(self):
+        rc = lib().fst_check_finite(self._ctx)
+        if rc == abi.FST_ERR_NONFINITE:
+            return False
+        self._check(rc, "check_finite")
+        return True
+
+    def synchronize(self):
+        self._check(lib().fst_synchronize(self._ctx), "synchronize")
+
+    def set_stream(self, stream_ptr):
+        self._check(lib().fst_set_stream(self._ctx, C.c_void_p(stream_ptr)), "set_stream")
+
+    def set_profiling(self, on=True):
+        self._check(lib().fst_set_profiling(self._ctx, int(bool(on))), "set_profiling")
+
+    def kernel_times(self):
+        """{kernel name: (launches, total ms)} since the last call."""
+        buf = (abi.FstKernelTime * 64)()
+        n = C.c_int(0)
+        self._check(lib().fst_kernel_times(self._ctx, buf, 64, C.byref(n)), "kernel_times")
+        return {buf[q].name.decode(): (buf[q].launches, buf[q].total_ms) for q in range(n.value)}
+
+    def stats(self):
+        s = abi.FstStats()
+        self._check(lib().fst_get_stats(self._ctx, C.byref(s)), "get_stats")
+        return {k: getattr(s, k) for k, _ in abi.FstStats._fields_ if k != "reserved"}
+
+
+class _RkFunc:
+    """Mirror of the reference's rk_func (src/rkfunction.hpp:36-69)."""
+
+    ndim = None
+
+    def __init__(self, cfg):
+        if cfg.ndim != self.ndim:
+            raise ValueError(f"{type(self).__name__} needs ndim={self.ndim}")
+        self.cf = cfg
+        self.solver = Solver(cfg)
+        self.t = 0
+
+    # var / dvar / varx as in the reference (host copies)
+    @property
+    def var(self):
+        return self.solver.get_state()
+
+    @var.setter
+    def var(self, U):
+        self.solver.set_state(U)
+
+    @property
+    def varx(self):
+        return self.solver.secondary()
+
+    def compute(self):
+        """R(U) into dvar; 3D applies BCs first (src/cart3d.cpp:221)."""
+        self.dvar = self.solver.compute_rhs()
+        return self.dvar
+
+    def preSim(self):
+        if self.ndim == 2:
+            self.solver.apply_bcs()  # src/cart2d.cpp:136-145
+
+    def preStep(self):
+        pass  # folded into rkAdvance below (2D BCs run inside fst_rk_step)
+
+    def postStep(self):
+        self.t += 1
+
+    def postSim(self):
+        self.solver.synchronize()
+
+
+class Cart3D(_RkFunc):
+    ndim = 3
+
+
+class Cart2D(_RkFunc):
+    ndim = 2
+
+
+def rkAdvance(cf, f):
+    """rkAdvance(cf, f) (src/rk.cpp:28-70), with the module's preStep BCs."""
+    f.solver.rk_step(1)

@@ -173,6 +173,20 @@ int fst_check_finite(fst_ctx* ctx);
 
 int fst_get_stats(const fst_ctx* ctx, fst_stats* out);
 
+/* Per-kernel device timing (the reference's per-region fiestaTimer,
+ * src/timer.hpp:52-119, reset/accumulated around kernels in
+ * src/cart3d.cpp:201-218).  With profiling on, every kernel launch is
+ * bracketed by CUDA events on the context's stream; fst_kernel_times
+ * synchronises, sums the times per kernel name since the last call, and
+ * clears them.  `count` receives the number of entries written (<= max). */
+typedef struct fst_kernel_time {
+  char name[48];
+  int64_t launches;
+  double total_ms;
+} fst_kernel_time;
+int fst_set_profiling(fst_ctx* ctx, int on);
+int fst_kernel_times(fst_ctx* ctx, fst_kernel_time* out, int max, int* count);
+
 /* Seeded initial conditions generated on the host (same on every platform;
  * no libm calls).  `kind`: FST_IC_*.  Writes the interior of U (LayoutLeft,
  * n = fst_state_size()); ghosts and C variables are set to zero. */
