@@ -141,12 +141,18 @@ def algorithmic_bytes(kernel, cfg):
     faces = (nci + 1) * (ncj + 1) * (nck + 1)
     inner = nci * ncj * nck
     tab = {
-        "prim3d": allc * (nv + 1 + 5 + ns + 1),
-        "flux3d": faces * (nv + 4 + 3 * nv),
-        "faces3d": faces * (3 + ns + 1 + 4 + 18 + 27),
-        "cell3d": inner * (3 * nv + 6 + 18 + 27 + 5 + 2 * nvt),
+        # plain FP64 kernels (8-byte words)
+        "prim3d": 8 * allc * (nv + 1 + 5 + ns + 1),
+        "flux3d": 8 * faces * (nv + 4 + 3 * nv),
+        "faces3d": 8 * faces * (3 + ns + 1 + 4 + 18 + 27),
+        "cell3d": 8 * inner * (3 * nv + 6 + 18 + 27 + 5 + 2 * nvt),
+        # mixed kernels: FP64 state in, FP32 primitives (+ FP64 p) out; the
+        # fused RHS reads the primitives once and the old state, writes the new
+        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + ns + 1 + 5) + 8),
+        "mrhs3d": inner * (4 * (nv + 1 + 3 + ns + 1 + 5) + 8 + 8 * nvt + 8 * nvt),
     }
-    return 8 * tab[kernel] if kernel in tab else None
+    tab["mrhs3d_hybrid"] = tab["mrhs3d"] + inner * 3
+    return tab.get(kernel)
 
 
 def read_traffic(kernel):
@@ -260,7 +266,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--modes", default="plain")
+    ap.add_argument("--modes", default="plain,mixed")
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample", type=int, default=128)

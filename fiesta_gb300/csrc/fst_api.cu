@@ -155,6 +155,13 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
   }
   P.mu2d = 2.928e-5;
   P.kheat2d = 0.026;
+  for (int s = 0; s < g.ns; ++s) {
+    P.cv_f[s] = (float)P.cv_s[s];
+    P.rm_f[s] = (float)(P.cp_s[s] - P.cv_s[s]);
+    P.mu_f[s] = (float)P.mu_s[s];
+    P.cv2_f[s] = (float)P.cv2_s[s];
+    P.cp2_f[s] = (float)P.cp2_s[s];
+  }
 }
 
 // Device bytes of the work arrays of each path, in doubles per cell.
@@ -208,7 +215,8 @@ int stage(fst_ctx* c, const double* Uin, const double* Uold, double* Unew, doubl
     n = fst_mixed_stage(c->g, c->P, c->cf, c->bm, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
                         &c->prof);
   else if (c->g.ndim == 3)
-    n = fst_plain3d_stage(c->g, c->P, c->b3, Uin, Uold, Unew, coef, Rout, c->stream, &c->prof);
+    n = fst_plain3d_stage(c->g, c->P, c->b3, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
+                          &c->prof);
   else
     n = fst_plain2d_stage(c->g, c->P, c->b2, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
                           &c->prof);
@@ -429,7 +437,7 @@ int fst_rk_step(fst_ctx* c, int nsteps) {
     const bool two_d = c->g.ndim == 2;
     if (two_d) rc = bcs(c, c->Ua);  // cart2d_func::preStep
     if (!rc && !two_d) rc = bcs(c, c->Ua);
-    if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, two_d);
+    if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, true);
     if (!rc && !two_d) rc = bcs(c, c->Ub);
     if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
     if (rc) return rc;

@@ -49,6 +49,10 @@ struct Phys {
   double dxmag;           // sqrt(dx^2+dy^2(+dz^2)): updateCeq cell size
   double mu2d;            // constant 2D viscosity 2.928e-5 (src/viscosity.hpp:62-63)
   double kheat2d;         // 2D heat conductivity 0.026 (src/viscosity.hpp:117)
+  // FP32 copies for the mixed path: cv_s, R_s = cp_s - cv_s, mu_s, and the
+  // stride-2 table constants
+  float cv_f[FST_MAX_SPECIES], rm_f[FST_MAX_SPECIES], mu_f[FST_MAX_SPECIES];
+  float cv2_f[FST_MAX_SPECIES], cp2_f[FST_MAX_SPECIES];
 };
 
 // --- order-preserving encoding of doubles for atomicMax -------------------
@@ -77,6 +81,12 @@ __device__ __forceinline__ double fst_warp_max(double v) {
     v = (w > v) ? w : v;  // NaN never wins, as in the reference reducer
   }
   return v;
+}
+
+// finiteness from the exponent bits (integer ops, not the FP64 pipe)
+__device__ __forceinline__ bool fst_finite(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7FF0000000000000ull) !=
+         0x7FF0000000000000ull;
 }
 
 // Linear index helpers

@@ -66,7 +66,7 @@ struct Plain3DBufs {
   unsigned long long* red;
 };
 int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* Uin,
-                      const double* Uold, double* Unew, double coef, double* Rout,
+                      const double* Uold, double* Unew, double coef, double* Rout, bool ghosts,
                       cudaStream_t st, Prof* prof);
 int fst_plain3d_secondary(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* U,
                           cudaStream_t st);
@@ -85,11 +85,27 @@ int fst_plain2d_secondary(const Geo& g, const Phys& P, const Plain2DBufs& b, con
 
 // fst_mixed.cu (FST_MODE_MIXED / FST_MODE_HYBRID)
 struct MixedBufs {
+  // FP32 primitives written by the mixed primitive pass
+  float *Q, *rho32, *vel32, *Y, *T32, *nrg, *C;
+  double* p64;  // FP64 pressure
+  // FP64 secondary outputs (fst_secondary)
   double *rho, *pr, *vel, *T;
-  void* work;          // path-specific work arrays
-  size_t work_bytes;
   unsigned long long* red;
-  unsigned long long* counters;  // hybrid: [0] faces, [1] WENO faces
+  unsigned long long* counters;  // hybrid: [0] faces classified, [1] routed to WENO
+  // hybrid smoothness classifier
+  bool hyb_active;
+  unsigned char* smooth;   // [cells][3] 1 = linear upwind on that face
+  void* mlp;               // device weights (fst_hybrid.cu)
+};
+struct MixedView {
+  const float* Q;    // [nv][cells] conserved variables, Q[ndim] = E + p
+  const float* rho;  // [cells]
+  const float* vel;  // [ndim][cells]
+  const double* p;   // [cells]
+  const float* Y;    // [ns][cells]
+  const float* nrg;  // [cells]
+  const float* C;    // [5][cells]
+  const float* T;    // [cells] (2D viscous heat flux)
 };
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);
@@ -101,3 +117,8 @@ int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const d
                         cudaStream_t st, const double** rho, const double** pr, const double** vel,
                         const double** T);
 double fst_mixed_flagged_fraction(const MixedBufs& b, cudaStream_t st);
+
+// fst_hybrid.cu (FST_MODE_HYBRID)
+int fst_hybrid_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc);
+int fst_hybrid_classify(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
+                        cudaStream_t st, Prof* prof, const unsigned char** smooth);

@@ -1,15 +1,678 @@
-// fst_mixed.cu — placeholder until the mixed-precision path lands.
+// fst_mixed.cu — mixed-precision right-hand side + RK stage (FST_MODE_MIXED)
+// and the fused kernel shared with the learned-hybrid variant
+// (FST_MODE_HYBRID) for sm_103a.
+//
+// Precision split:
+//   FP64  the conserved state, the RK stage combine, the pressure recovery
+//         p = (gamma-1)*(E - KE) (the low-Mach cancellation), the stored
+//         pressure and its 4th-order gradient, E + p
+//   FP32  mixture properties from FP32 mass fractions, velocities, WENO5
+//         reconstruction and fluxes, viscous stress, C-equation terms
+//
+// Two kernels per stage:
+//   k_mprim    all cells: FP64 state -> FP32 primitives (+ FP64 p), and the
+//              C-equation maxima (maxS, maxCh) by warp max + atomicMax
+//   k_mrhs3d   a fused 2.5D stencil.  A 32x8 thread tile marches along k;
+//              thread (tx, ty) owns column (i0-1+tx, j0-1+ty) and computes the
+//              faces at i+1/2, j+1/2, k+1/2 once each.  Every face carries nv
+//              FP32 values G_v = F_v - V_v/d: the WENO flux F_v and, for the
+//              momenta and energy, the viscous stress and C-equation tensor
+//              terms V_v of the reference (applyViscousTerm*, applyCeq), which
+//              have the same (face(i) - face(i-1))/d form as the flux
+//              divergence.  The left x face comes from lane-1 by shuffle, the
+//              lower y face from the row below through shared memory, the
+//              back z face from the previous plane in registers.  The cell
+//              then adds the pressure gradient (FP64), buoyancy and the
+//              C-equation source and writes Unew = Uold + coef*R in FP64.
+//              Face and stress arrays never go to HBM.
+// Kernels are instantiated per variable count so every per-variable array
+// lives in registers.  The equations, quirks included, are the reference's
+// (src/flux.hpp, src/viscosity.hpp, src/ceq3d.hpp, src/ceq.hpp,
+// src/presgrad.hpp, src/buoyancy.hpp); only the arithmetic precision differs.
+// The error against the FP64 oracle is measured by tests/test_gpu_mixed.py.
 #include "fst_internal.h"
-size_t fst_mixed_work_doubles_per_cell(const fst_config&, const Geo&) { return 0; }
-int fst_mixed_alloc(const fst_config&, const Geo&, MixedBufs&, const fst_alloc_fn&) {
-  return FST_ERR_UNSUPPORTED;
+
+namespace {
+
+constexpr int TX = 32;  // tile width (threads along i)
+constexpr int TY = 8;   // tile height (threads along j)
+constexpr int KZ = 16;  // planes per block along k
+constexpr int NVMAX = 4 + FST_MAX_SPECIES;
+
+// ---------------------------------------------------------------------------
+// primitives
+// ---------------------------------------------------------------------------
+template <int NDIM>
+__global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __restrict__ U,
+                                               float* __restrict__ Q, float* __restrict__ rho,
+                                               float* __restrict__ vel, double* __restrict__ pr,
+                                               float* __restrict__ Y, float* __restrict__ nrg,
+                                               float* __restrict__ Cc, float* __restrict__ T,
+                                               unsigned long long* __restrict__ red) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long sv = g.sv;
+  float lS = -3.0e38f;
+  double lC = -1.7976931348623157e308;
+  if (c < sv) {
+    const int s0 = NDIM + 1;  // first species index
+    float r = 0.f;
+    for (int s = 0; s < P.ns; ++s) r += (float)U[c + sv * (s0 + s)];
+    const float ri = 1.0f / r;
+    float Cv = 0.f, Rm = 0.f, Cv2 = 0.f, Cp2 = 0.f;
+    for (int s = 0; s < P.ns; ++s) {
+      const float rs = (float)U[c + sv * (s0 + s)];
+      const float ys = rs * ri;
+      Cv += ys * P.cv_f[s];
+      Rm += ys * P.rm_f[s];
+      if (NDIM == 2) {
+        Cv2 += ys * P.cv2_f[s];
+        Cp2 += ys * P.cp2_f[s];
+      }
+      if (Y) Y[c + sv * s] = ys;
+      Q[c + sv * (s0 + s)] = rs;
+    }
+    const float gm1 = Rm / Cv;  // gamma - 1 of the mixture
+    float usq = 0.f, msq = 0.f;
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+      const float m = (float)U[c + sv * d];
+      const float u = m * ri;
+      usq += u * u;
+      msq += m * m;
+      vel[c + sv * d] = u;
+      Q[c + sv * d] = m;
+    }
+    const double E = U[c + sv * NDIM];
+    const float ke = 0.5f * msq * ri;
+    const double p = (double)gm1 * (E - (double)ke);  // FP64 pressure recovery
+    pr[c] = p;
+    Q[c + sv * NDIM] = (float)(E + p);
+    rho[c] = r;
+    if (T) T[c] = (float)p * ri / Rm;
+    if (nrg) nrg[c] = (float)E * ri - 0.5f * r * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
+    if (Cc)
+      for (int n = 0; n < 5; ++n) Cc[c + sv * n] = (float)U[c + sv * (P.nv + n)];
+    if (red) {
+      const int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj);
+      const int k = NDIM == 3 ? (int)(c / g.sz) : g.ng;
+      const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
+                      (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
+      if (in) {
+        float s;
+        if (NDIM == 3) {
+          s = sqrtf((1.0f + gm1) * (float)p * ri) + sqrtf(msq) * ri;
+        } else {
+          // maxWaveSpeed2D: stride-2 species table, momentum without /rho
+          s = sqrtf(Cp2 / Cv2 * (float)p * ri) + sqrtf(msq);
+        }
+        if (s > lS) lS = s;
+        const double ch = fabs(U[c + sv * (P.nv + 1)]);
+        if (ch > lC) lC = ch;
+      }
+    }
+  }
+  if (red) {
+    const double ds = fst_warp_max((double)lS);
+    lC = fst_warp_max(lC);
+    if ((threadIdx.x & 31) == 0) {
+      if (ds > -1e38) atomicMax(&red[0], fst_key(ds));
+      atomicMax(&red[1], fst_key(lC));
+    }
+  }
 }
-int fst_mixed_stage(const Geo&, const Phys&, const fst_config&, const MixedBufs&, const double*,
-                    const double*, double*, double, double*, bool, cudaStream_t, Prof*) {
-  return 0;
+
+// ---------------------------------------------------------------------------
+// FP32 WENO5-JS with the reference's weights (src/flux.hpp:241-266); the
+// nonlinear weights are scaled by the smallest (eps+beta) so that no square
+// overflows or underflows in FP32 (the normalised weights are unchanged).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float weno_f(float f1, float f2, float f3, float f4, float f5) {
+  const float eps = 1e-6f;
+  float a1 = f1 - 2.0f * f2 + f3, a2 = f1 - 4.0f * f2 + 3.0f * f3;
+  const float b1 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
+  a1 = f2 - 2.0f * f3 + f4;
+  a2 = f2 - f4;
+  const float b2 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
+  a1 = f3 - 2.0f * f4 + f5;
+  a2 = 3.0f * f3 - 4.0f * f4 + f5;
+  const float b3 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
+  const float e1 = eps + b1, e2 = eps + b2, e3 = eps + b3;
+  const float mn = fminf(e1, fminf(e2, e3));
+  const float r1 = __fdividef(mn, e1), r2 = __fdividef(mn, e2), r3 = __fdividef(mn, e3);
+  const float w1 = 0.1f * r1 * r1, w2 = 0.6f * r2 * r2, w3 = 0.3f * r3 * r3;
+  const float p1 = (1.0f / 3.0f) * f1 + (-7.0f / 6.0f) * f2 + (11.0f / 6.0f) * f3;
+  const float p2 = (-1.0f / 6.0f) * f2 + (5.0f / 6.0f) * f3 + (1.0f / 3.0f) * f4;
+  const float p3 = (1.0f / 3.0f) * f3 + (5.0f / 6.0f) * f4 + (-1.0f / 6.0f) * f5;
+  return __fdividef(w1 * p1 + w2 * p2 + w3 * p3, w1 + w2 + w3);
 }
-int fst_mixed_secondary(const Geo&, const Phys&, const MixedBufs&, const double*, cudaStream_t,
-                        const double**, const double**, const double**, const double**) {
-  return 0;
+
+// The linear 5th-order upwind reconstruction: WENO5 with the optimal weights
+// d = (0.1, 0.6, 0.3), i.e. (2 f1 - 13 f2 + 47 f3 + 27 f4 - 3 f5) / 60.
+__device__ __forceinline__ float upwind5_f(float f1, float f2, float f3, float f4, float f5) {
+  return (1.0f / 30.0f) * f1 + (-13.0f / 60.0f) * f2 + (47.0f / 60.0f) * f3 +
+         (27.0f / 60.0f) * f4 + (-1.0f / 20.0f) * f5;
 }
-double fst_mixed_flagged_fraction(const MixedBufs&, cudaStream_t) { return 0.0; }
+
+struct FaceCtx {
+  float rd[3];   // 1/dx, 1/dy, 1/dz
+  float r4d[3];  // 1/(4dx) ...
+  float alpha;
+};
+
+__device__ __forceinline__ FaceCtx make_ctx(const Phys& P, const unsigned long long* red,
+                                            float* maxS) {
+  FaceCtx fc;
+  fc.rd[0] = (float)(1.0 / P.dx);
+  fc.rd[1] = (float)(1.0 / P.dy);
+  fc.rd[2] = (float)(1.0 / P.dz);
+  fc.r4d[0] = 0.25f * fc.rd[0];
+  fc.r4d[1] = 0.25f * fc.rd[1];
+  fc.r4d[2] = 0.25f * fc.rd[2];
+  fc.alpha = 0.f;
+  *maxS = 0.f;
+  if (P.ceq) {
+    const double maxCh = fst_unkey(red[1]);
+    fc.alpha = (float)((P.dxmag2 / (maxCh + 1.0e-6)) * P.alpha);  // src/cart3d.cpp:285
+    *maxS = (float)fst_unkey(red[0]);
+  }
+  return fc;
+}
+
+// ---------------------------------------------------------------------------
+// Face terms of one 3D face (normal f) owned by cell index c: G[v], v < nv.
+// ---------------------------------------------------------------------------
+template <int NV, bool HYB>
+__device__ __forceinline__ void face3d(const Geo& g, const Phys& P, const MixedView& M,
+                                       const FaceCtx& fc, long long c, int f, bool smooth,
+                                       int nv, float* G) {
+  const long long sv = g.sv;
+  const long long sf = f == 0 ? 1 : f == 1 ? g.sy : g.sz;
+  const float* un = M.vel + sv * f;
+  const float uf = (-un[c + 2 * sf] + 7.0f * un[c + sf] + 7.0f * un[c] - un[c - sf]) * (1.0f / 12.0f);
+  const bool neg = uf < 0.0f;
+  const long long c0 = neg ? c + 3 * sf : c - 2 * sf;
+  const long long o = neg ? -sf : sf;
+  const float scale = uf * fc.rd[f];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    if (NV == NVMAX && v >= nv) break;
+    const float* q = M.Q + sv * v;
+    const float f1 = __ldg(q + c0), f2 = __ldg(q + c0 + o), f3 = __ldg(q + c0 + 2 * o),
+                f4 = __ldg(q + c0 + 3 * o), f5 = __ldg(q + c0 + 4 * o);
+    const float rec = (HYB && smooth) ? upwind5_f(f1, f2, f3, f4, f5) : weno_f(f1, f2, f3, f4, f5);
+    G[v] = scale * rec;
+  }
+  if (!(P.visc || P.ceq)) return;
+  // velocity gradients at the face: gr[d][w] = d u_w / d x_d (the stress and
+  // C-equation gradient expressions of the reference are the same ones)
+  float gr[3][3];
+#pragma unroll
+  for (int w = 0; w < 3; ++w) {
+    const float* u = M.vel + sv * w;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d == f) {
+        gr[d][w] = (__ldg(u + c + sf) - __ldg(u + c)) * fc.rd[d];
+      } else {
+        const long long st = d == 0 ? 1 : d == 1 ? g.sy : g.sz;
+        gr[d][w] = ((__ldg(u + c + sf + st) + __ldg(u + c + st)) -
+                    (__ldg(u + c + sf - st) + __ldg(u + c - st))) * fc.r4d[d];
+      }
+    }
+  }
+  float V[4] = {0.f, 0.f, 0.f, 0.f};  // x-, y-, z-momentum, energy
+  if (P.visc) {
+    float mu = 0.f;
+    for (int s = 0; s < P.ns; ++s)
+      mu += 0.5f * (__ldg(M.Y + c + sf + sv * s) + __ldg(M.Y + c + sv * s)) * P.mu_f[s];
+    const float div = gr[0][0] + gr[1][1] + gr[2][2];
+    float e = 0.f;
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {
+      // stress components on this face (calculateStressTensor{x,y,z}3dv)
+      const float Tw = (w == f) ? (2.0f / 3.0f) * mu * (3.0f * gr[f][f] - div)
+                                : mu * (gr[f][w] + gr[w][f]);
+      const float* u = M.vel + sv * w;
+      e += 0.5f * (__ldg(u + c + sf) + __ldg(u + c)) * Tw;
+      V[w] += Tw;
+    }
+    V[3] = e;
+  }
+  if (P.ceq) {
+    const float r = 0.5f * (__ldg(M.rho + c) + __ldg(M.rho + c + sf));
+    const float chat = 0.5f * (__ldg(M.C + c + sv) + __ldg(M.C + c + sf + sv));
+    float cn[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      cn[q] = 0.5f * (__ldg(M.C + c + sv * (2 + q)) + __ldg(M.C + c + sf + sv * (2 + q)));
+    const float cmag = 1.0e-6f + cn[0] * cn[0] + cn[1] * cn[1] + cn[2] * cn[2];
+    const float rc = __fdividef(1.0f, cmag);
+    const float arc = fc.alpha * r * chat;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float base = arc * ((f == d ? 1.0f : 0.0f) - cn[f] * cn[d] * rc);
+#pragma unroll
+      for (int w = 0; w < 3; ++w) V[w] += base * gr[d][w];
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < 4; ++w) G[w] -= V[w] * fc.rd[f];
+}
+
+__device__ __forceinline__ bool smooth_at(const unsigned char* map, long long c, int f) {
+  return map != nullptr && map[c * 3 + f] != 0;
+}
+
+// ---------------------------------------------------------------------------
+// k_mrhs3d: fused 2.5D RHS + RK stage.  Rout (FP64) instead of the update
+// when computing a bare right-hand side.
+// ---------------------------------------------------------------------------
+template <int NV, bool HYB>
+__global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
+                                                    const unsigned long long* __restrict__ red,
+                                                    const unsigned char* __restrict__ smap,
+                                                    const double* Uold, double* Unew, double coef,
+                                                    double* __restrict__ Rout) {
+  __shared__ float sG[TY][TX][NV];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = g.ng - 1 + blockIdx.x * (TX - 1) + tx;  // column of this thread
+  const int j = g.ng - 1 + blockIdx.y * (TY - 1) + ty;
+  const int kc0 = g.ng + blockIdx.z * KZ;
+  const int kc1 = min(kc0 + KZ, g.ngk - g.ng);
+  const long long sv = g.sv, sy = g.sy, sz = g.sz;
+  const int nv = P.nv;
+  float maxS;
+  const FaceCtx fc = make_ctx(P, red, &maxS);
+  const bool fi = i <= g.ngi - g.ng - 1;  // x face i+1/2 exists
+  const bool fj = j <= g.ngj - g.ng - 1;  // y face j+1/2 exists
+  const bool ci = tx >= 1 && i >= g.ng && i < g.ngi - g.ng;
+  const bool cj = ty >= 1 && j >= g.ng && j < g.ngj - g.ng;
+  const bool cell_col = ci && cj;
+
+  float Gz[NV], Gx[NV], Gy[NV], Gzn[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) Gz[v] = Gx[v] = Gy[v] = Gzn[v] = 0.f;
+  if (cell_col) {  // prologue: z face at kc0 - 1/2
+    const long long c = (long long)i + sy * j + sz * (kc0 - 1);
+    face3d<NV, HYB>(g, P, M, fc, c, 2, HYB && smooth_at(smap, c, 2), nv, Gz);
+  }
+  for (int k = kc0; k < kc1; ++k) {
+    const long long c = (long long)i + sy * j + sz * k;
+    if (fi && cj) face3d<NV, HYB>(g, P, M, fc, c, 0, HYB && smooth_at(smap, c, 0), nv, Gx);
+    if (fj && ci) face3d<NV, HYB>(g, P, M, fc, c, 1, HYB && smooth_at(smap, c, 1), nv, Gy);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sG[ty][tx][v] = Gy[v];
+    __syncthreads();
+    if (cell_col) face3d<NV, HYB>(g, P, M, fc, c, 2, HYB && smooth_at(smap, c, 2), nv, Gzn);
+    float R[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float gxl = __shfl_up_sync(0xffffffffu, Gx[v], 1);
+      R[v] = 0.f;
+      if (cell_col) R[v] = -((Gx[v] - gxl) + (Gy[v] - sG[ty - 1][tx][v]) + (Gzn[v] - Gz[v]));
+    }
+    if (cell_col) {
+      // pressure gradient in FP64 (reference quirk: z spacing is dy)
+      const double* p = M.p;
+      const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) / P.d12x;
+      const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) / P.d12y;
+      const double dpz = (p[c - 2 * sz] - 8.0 * p[c - sz] + 8.0 * p[c + sz] - p[c + 2 * sz]) / P.d12pz;
+      double Rd[4] = {(double)R[0] - dpx, (double)R[1] - dpy, (double)R[2] - dpz, (double)R[3]};
+      if (P.buoyancy) {
+        const float f = -(float)P.g * (M.rho[c] - (float)P.rho_ref);
+        Rd[1] += f;
+        Rd[3] += (double)(M.vel[c + sv] * f);
+      }
+      auto emit = [&](int v, double Rv) {
+        if (Rout) Rout[c + sv * v] = Rv;
+        else Unew[c + sv * v] = Uold[c + sv * v] + coef * Rv;
+      };
+#pragma unroll
+      for (int w = 0; w < 4; ++w) emit(w, Rd[w]);
+#pragma unroll
+      for (int v = 4; v < NV; ++v) {
+        if (NV == NVMAX && v >= nv) break;
+        emit(v, (double)R[v]);
+      }
+      if (P.ceq) {
+        const float r12x = (float)(1.0 / P.d12x), r12y = (float)(1.0 / P.d12y),
+                    r12z = (float)(1.0 / P.d12z);
+        auto d4 = [&](const float* a, long long st, float r12) {
+          return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
+        };
+        const float dxr = d4(M.rho, 1, r12x), dyr = d4(M.rho, sy, r12y), dzr = d4(M.rho, sz, r12z);
+        const float dxe = d4(M.nrg, 1, r12x), dye = d4(M.nrg, sy, r12y), dze = d4(M.nrg, sz, r12z);
+        const float divu = d4(M.vel, 1, r12x) + d4(M.vel + sv, sy, r12y) + d4(M.vel + 2 * sv, sz, r12z);
+        const float rgrad = sqrtf(dxr * dxr + dyr * dyr + dzr * dzr);
+        const float dnednr = (dxr * dxe + dyr * dye + dzr * dze) * (dxr * dxr + dyr * dyr + dzr * dzr);
+        const bool ind = dnednr < 0.0f;
+        const float Gs[5] = {divu < 0.f && !ind ? rgrad : 0.f, ind ? rgrad : 0.f, dxr, dyr, dzr};
+        const float dxm = (float)P.dxmag;
+        const float src = maxS / ((float)P.eps * dxm);
+        const float dif = (float)P.kap * maxS * dxm;
+#pragma unroll
+        for (int n = 0; n < 5; ++n) {
+          const float* Cn = M.C + sv * n;
+          const float cc = Cn[c];
+          const float lap = (Cn[c - 1] - 2.0f * cc + Cn[c + 1]) * fc.rd[0] +
+                            (Cn[c - sy] - 2.0f * cc + Cn[c + sy]) * fc.rd[1] +
+                            (Cn[c - sz] - 2.0f * cc + Cn[c + sz]) * fc.rd[2];
+          emit(nv + n, (double)(src * (Gs[n] - cc) + dif * lap));
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Gz[v] = Gzn[v];
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2D face terms of cart2d (src/flux.hpp:23-106, src/viscosity.hpp:25-199,
+// src/ceq.hpp:200-293) with their quirks, in FP32.
+// ---------------------------------------------------------------------------
+template <int NV, bool HYB>
+__device__ __forceinline__ void face2d(const Geo& g, const Phys& P, const MixedView& M,
+                                       const FaceCtx& fc, long long c, int f, bool smooth,
+                                       int nv, float* G) {
+  const long long sv = g.sv, sx = 1, sy = g.sy;
+  const long long sf = f == 0 ? sx : sy;
+  const float* un = M.vel + sv * f;
+  const float uf = (-un[c + 2 * sf] + 7.0f * un[c + sf] + 7.0f * un[c] - un[c - sf]) * (1.0f / 12.0f);
+  const bool neg = uf < 0.0f;
+  const long long c0 = neg ? c + 3 * sf : c - 2 * sf;
+  const long long o = neg ? -sf : sf;
+  const float scale = uf * fc.rd[f];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    if (NV == NVMAX && v >= nv) break;
+    const float* q = M.Q + sv * v;
+    const float f1 = __ldg(q + c0), f2 = __ldg(q + c0 + o), f3 = __ldg(q + c0 + 2 * o),
+                f4 = __ldg(q + c0 + 3 * o), f5 = __ldg(q + c0 + 4 * o);
+    G[v] = scale * ((HYB && smooth) ? upwind5_f(f1, f2, f3, f4, f5) : weno_f(f1, f2, f3, f4, f5));
+  }
+  if (!(P.visc || P.ceq)) return;
+  const float* u = M.vel;
+  const float* v = M.vel + sv;
+  float V[3] = {0.f, 0.f, 0.f};  // x-, y-momentum, energy
+  if (P.visc) {
+    const float mu = (float)P.mu2d;
+    float dudx, dvdx, dudy, dvdy;
+    if (f == 0) {
+      dudx = (u[c + sx] - u[c]) * fc.rd[0];
+      dvdx = (v[c + sx] - v[c]) * fc.rd[0];
+      dudy = ((u[c + sy] + u[c + sx + sy]) - (v[c - sy] + u[c + sx - sy])) * fc.r4d[1];  // vel(i,j-1,1)
+      dvdy = ((v[c + sy] + v[c + sx + sy]) - (v[c - sy] + v[c + sx - sy])) * fc.r4d[1];
+    } else {
+      dudx = ((u[c + sx] + u[c + sx + sy]) - (u[c - sx] + u[c - sx + sy])) * fc.r4d[0];
+      dvdx = ((v[c + sx] + v[c + sx + sy]) - (v[c - sx] + v[c - sx + sy])) * fc.r4d[0];
+      dudy = (u[c + sy] - u[c]) * fc.rd[1];
+      dvdy = (v[c + sy] - v[c]) * fc.rd[1];
+    }
+    const float sxx = (2.0f / 3.0f) * mu * (2.0f * dudx - dvdy);
+    const float syy = (2.0f / 3.0f) * mu * (2.0f * dvdy - dudx);
+    const float sxy = mu * (dudy + dvdx);
+    const float sn = f == 0 ? sxx : sxy;  // x-momentum component on this face
+    const float st = f == 0 ? sxy : syy;  // y-momentum component
+    const float q = -(float)P.kheat2d * (M.T[c + sf] - M.T[c]) * fc.rd[f];
+    V[0] = sn;
+    V[1] = st;
+    V[2] = 0.5f * (u[c + sf] + u[c]) * sn + 0.5f * (v[c + sf] + v[c]) * st - q;
+  }
+  if (P.ceq) {
+    const float r = 0.5f * (M.rho[c] + M.rho[c + sf]);
+    const float chat = 0.5f * (M.C[c + sv] + M.C[c + sf + sv]);
+    const float ct0 = 0.5f * (M.C[c + 2 * sv] + M.C[c + sf + 2 * sv]);
+    const float ct1 = 0.5f * (M.C[c + 3 * sv] + M.C[c + sf + 3 * sv]);
+    const float rct = __fdividef(1.0f, ct0 * ct0 + ct1 * ct1 + 1.0e-6f);
+    const float ctf = f == 0 ? ct0 : ct1;
+    const float arc = fc.alpha * r * chat * ctf * rct;
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const float* vw = M.vel + sv * w;
+      float g0, g1;
+      if (f == 0) {
+        g0 = (vw[c + sx] - vw[c]) * fc.rd[0];
+        g1 = ((vw[c + sy] + vw[c + sx + sy]) - (vw[c - sy] + vw[c + sx - sy])) * fc.r4d[1];
+      } else {
+        g0 = ((vw[c + sx] + vw[c + sx + sy]) - (vw[c - sx] + vw[c - sx + sy])) * fc.r4d[0];
+        g1 = (vw[c + sy] - vw[c]) * fc.rd[1];
+      }
+      V[w] += arc * (ct0 * g0 + ct1 * g1);
+    }
+  }
+  G[0] -= V[0] * fc.rd[f];
+  G[1] -= V[1] * fc.rd[f];
+  G[2] -= V[2] * fc.rd[f];
+}
+
+template <int NV, bool HYB>
+__global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
+                                                    const unsigned long long* __restrict__ red,
+                                                    const unsigned char* __restrict__ smap,
+                                                    const double* Uold, double* Unew, double coef,
+                                                    double* __restrict__ Rout) {
+  __shared__ float sG[TY][TX][NV];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = g.ng - 1 + blockIdx.x * (TX - 1) + tx;
+  const int j = g.ng - 1 + blockIdx.y * (TY - 1) + ty;
+  const long long sv = g.sv, sy = g.sy;
+  const int nv = P.nv;
+  float maxS;
+  FaceCtx fc = make_ctx(P, red, &maxS);
+  fc.rd[2] = fc.rd[0];
+  const bool fi = i <= g.ngi - g.ng - 1;
+  const bool fj = j <= g.ngj - g.ng - 1;
+  const bool ci = tx >= 1 && i >= g.ng && i < g.ngi - g.ng;
+  const bool cj = ty >= 1 && j >= g.ng && j < g.ngj - g.ng;
+  const long long c = (long long)i + sy * j;
+  float Gx[NV], Gy[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) Gx[v] = Gy[v] = 0.f;
+  if (fi && cj) face2d<NV, HYB>(g, P, M, fc, c, 0, HYB && smooth_at(smap, c, 0), nv, Gx);
+  if (fj && ci) face2d<NV, HYB>(g, P, M, fc, c, 1, HYB && smooth_at(smap, c, 1), nv, Gy);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) sG[ty][tx][v] = Gy[v];
+  __syncthreads();
+  float R[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const float gxl = __shfl_up_sync(0xffffffffu, Gx[v], 1);
+    R[v] = 0.f;
+    if (ci && cj) R[v] = -((Gx[v] - gxl) + (Gy[v] - sG[ty - 1][tx][v]));
+  }
+  if (!(ci && cj)) return;
+  const double* p = M.p;
+  const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) / P.d12x;
+  const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) / P.d12y;
+  double Rd[3] = {(double)R[0] - dpx, (double)R[1] - dpy, (double)R[2]};
+  if (P.buoyancy) {
+    const float rhop = M.rho[c] - (float)P.rho_ref;
+    if (rhop >= 1e-6f || rhop <= -1e-6f) {
+      const float f = -(float)P.g * rhop;
+      const float vb = M.Q[c + sv] / M.Q[c + 3 * sv];  // m_y / rho_1 (reference)
+      Rd[1] += f;
+      Rd[2] += (double)(fabsf(vb) * f);
+    }
+  }
+  auto emit = [&](int v, double Rv) {
+    if (Rout) Rout[c + sv * v] = Rv;
+    else Unew[c + sv * v] = Uold[c + sv * v] + coef * Rv;
+  };
+#pragma unroll
+  for (int w = 0; w < 3; ++w) emit(w, Rd[w]);
+#pragma unroll
+  for (int v = 3; v < NV; ++v) {
+    if (NV == NVMAX && v >= nv) break;
+    emit(v, (double)R[v]);
+  }
+  if (P.ceq) {
+    const float r12x = (float)(1.0 / P.d12x), r12y = (float)(1.0 / P.d12y);
+    auto d4 = [&](const float* a, long long st, float r12) {
+      return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
+    };
+    const float dxr = d4(M.rho, 1, r12x), dyr = d4(M.rho, sy, r12y);
+    const float dxe = d4(M.nrg, 1, r12x), dye = d4(M.nrg, sy, r12y);
+    const float divu = d4(M.vel, 1, r12x) + d4(M.vel + sv, sy, r12y);
+    const float rgrad = sqrtf(dxr * dxr + dyr * dyr);
+    const float dnednr = (dxr * dxe + dyr * dye) * (dxr * dxr + dyr * dyr);
+    const bool i1 = dnednr < 0.0f;
+    const float Gs[4] = {(!i1 && divu < 0.f) ? rgrad : 0.f, i1 ? rgrad : 0.f, -dyr, dxr};
+    const float dxm = (float)P.dxmag;
+    const float src = maxS / ((float)P.eps * dxm);
+    const float dif = (float)P.kap * maxS * dxm;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const float* Cn = M.C + sv * n;
+      const float cc = Cn[c];
+      const float lap = (Cn[c + 1] - 2.0f * cc + Cn[c - 1]) * fc.rd[0] +
+                        (Cn[c + sy] - 2.0f * cc + Cn[c - sy]) * fc.rd[1];
+      emit(nv + n, (double)(src * (Gs[n] - cc) + dif * lap));
+    }
+    emit(nv + 4, 0.0);
+  }
+}
+
+// ghost cells of the stage-1 buffer: U1 = U + (0.5*dt)*0 (src/rk.cpp:42-50)
+__global__ void k_mghost(Geo g, const double* __restrict__ Uold, double* __restrict__ Unew) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.sv) return;
+  const int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj);
+  const int k = g.ndim == 3 ? (int)(c / g.sz) : g.ng;
+  const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
+                  (g.ndim == 2 || (k >= g.ng && k < g.ngk - g.ng));
+  if (in) return;
+  for (int v = 0; v < g.nvt; ++v) Unew[c + g.sv * v] = Uold[c + g.sv * v];
+}
+
+inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
+
+// Launch the fused RHS for a compile-time variable count.
+template <int NV, bool HYB>
+void launch_rhs(const Geo& g, const Phys& P, const MixedView& M, const unsigned long long* red,
+                const unsigned char* smap, const double* Uold, double* Unew, double coef,
+                double* Rout, cudaStream_t st) {
+  const dim3 blk(TX, TY, 1);
+  if (g.ndim == 3) {
+    const dim3 grd(cdiv(g.nci, TX - 1), cdiv(g.ncj, TY - 1), cdiv(g.nck, KZ));
+    k_mrhs3d<NV, HYB><<<grd, blk, 0, st>>>(g, P, M, red, smap, Uold, Unew, coef, Rout);
+  } else {
+    const dim3 grd(cdiv(g.nci, TX - 1), cdiv(g.ncj, TY - 1), 1);
+    k_mrhs2d<NV, HYB><<<grd, blk, 0, st>>>(g, P, M, red, smap, Uold, Unew, coef, Rout);
+  }
+}
+
+template <bool HYB>
+void dispatch_rhs(const Geo& g, const Phys& P, const MixedView& M, const unsigned long long* red,
+                  const unsigned char* smap, const double* Uold, double* Unew, double coef,
+                  double* Rout, cudaStream_t st) {
+  switch (g.nv) {
+    case 4: launch_rhs<4, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+    case 5: launch_rhs<5, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+    case 6: launch_rhs<6, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+    case 7: launch_rhs<7, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+    case 8: launch_rhs<8, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+    case 9: launch_rhs<9, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+    default: launch_rhs<NVMAX, HYB>(g, P, M, red, smap, Uold, Unew, coef, Rout, st); break;
+  }
+}
+
+}  // namespace
+
+size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g) {
+  // floats: Q nv, rho, vel ndim, Y ns, nrg, C 5, T; doubles: p and the
+  // FP64 secondary outputs (rho, p, vel, T); hybrid: 3 map bytes
+  const size_t fl = g.nv + 1 + g.ndim + g.ns + 1 + 5 + 1;
+  (void)cf;
+  return (fl + 1) / 2 + 1 + (size_t)(g.ndim + 3) + 1;
+}
+
+int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc) {
+  const size_t n = (size_t)g.sv;
+  int rc = 0;
+  auto A = [&](void** p, size_t bytes) {
+    if (!rc) rc = alloc(p, bytes);
+  };
+  A((void**)&b.Q, sizeof(float) * n * g.nv);
+  A((void**)&b.rho32, sizeof(float) * n);
+  A((void**)&b.vel32, sizeof(float) * n * g.ndim);
+  A((void**)&b.p64, sizeof(double) * n);
+  if (cf.visc && g.ndim == 3) A((void**)&b.Y, sizeof(float) * n * g.ns);
+  if (cf.visc && g.ndim == 2) A((void**)&b.T32, sizeof(float) * n);
+  if (cf.ceq) {
+    A((void**)&b.nrg, sizeof(float) * n);
+    A((void**)&b.C, sizeof(float) * n * 5);
+  }
+  A((void**)&b.rho, sizeof(double) * n);
+  A((void**)&b.pr, sizeof(double) * n);
+  A((void**)&b.vel, sizeof(double) * n * g.ndim);
+  A((void**)&b.T, sizeof(double) * n);
+  A((void**)&b.red, sizeof(unsigned long long) * 2);
+  A((void**)&b.counters, sizeof(unsigned long long) * 4);
+  if (!rc && cf.mode == FST_MODE_HYBRID) rc = fst_hybrid_alloc(cf, g, b, alloc);
+  return rc;
+}
+
+int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
+                    const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
+                    bool ghosts, cudaStream_t st, Prof* prof) {
+  int n = 0;
+  if (P.ceq) {
+    const unsigned long long init[2] = {FST_KEY_LOWEST, FST_KEY_LOWEST};
+    cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  }
+  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.Y, b.nrg, b.C, b.T32};
+  if (g.ndim == 3) {
+    FST_LAUNCH(prof, "mprim3d", st, n,
+               k_mprim<3><<<cdiv(g.sv, 256), 256, 0, st>>>(
+                   g, P, Uin, b.Q, b.rho32, b.vel32, b.p64, P.visc ? b.Y : nullptr,
+                   P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, nullptr,
+                   P.ceq ? b.red : nullptr));
+  } else {
+    FST_LAUNCH(prof, "mprim2d", st, n,
+               k_mprim<2><<<cdiv(g.sv, 256), 256, 0, st>>>(
+                   g, P, Uin, b.Q, b.rho32, b.vel32, b.p64, nullptr, P.ceq ? b.nrg : nullptr,
+                   P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr, P.ceq ? b.red : nullptr));
+  }
+  const bool hyb = cf.mode == FST_MODE_HYBRID && b.hyb_active;
+  const unsigned char* smooth = nullptr;
+  if (hyb) n += fst_hybrid_classify(g, P, b, M, st, prof, &smooth);
+  if (hyb)
+    FST_LAUNCH(prof, g.ndim == 3 ? "mrhs3d_hybrid" : "mrhs2d_hybrid", st, n,
+               dispatch_rhs<true>(g, P, M, b.red, smooth, Uold, Unew, coef, Rout, st));
+  else
+    FST_LAUNCH(prof, g.ndim == 3 ? "mrhs3d" : "mrhs2d", st, n,
+               dispatch_rhs<false>(g, P, M, b.red, nullptr, Uold, Unew, coef, Rout, st));
+  if (ghosts && !Rout)
+    FST_LAUNCH(prof, "mghost", st, n, k_mghost<<<cdiv(g.sv, 256), 256, 0, st>>>(g, Uold, Unew));
+  return n;
+}
+
+int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const double* U,
+                        cudaStream_t st, const double** rho, const double** pr, const double** vel,
+                        const double** T) {
+  int n;
+  if (g.ndim == 3) {
+    Plain3DBufs p3{};
+    p3.rho = b.rho; p3.pr = b.pr; p3.vel = b.vel; p3.T = b.T;
+    n = fst_plain3d_secondary(g, P, p3, U, st);
+  } else {
+    Plain2DBufs p2{};
+    p2.rho = b.rho; p2.pr = b.pr; p2.vel = b.vel; p2.T = b.T;
+    n = fst_plain2d_secondary(g, P, p2, U, st);
+  }
+  *rho = b.rho;
+  *pr = b.pr;
+  *vel = b.vel;
+  *T = b.T;
+  return n;
+}
+
+double fst_mixed_flagged_fraction(const MixedBufs& b, cudaStream_t st) {
+  if (!b.hyb_active || !b.counters) return 0.0;
+  unsigned long long h[2] = {0, 0};
+  if (cudaMemcpyAsync(h, b.counters, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return 0.0;
+  return h[0] ? (double)h[1] / (double)h[0] : 0.0;
+}

@@ -124,9 +124,15 @@ __global__ void __launch_bounds__(128) k_flux2d(Geo g, Phys P, const double* __r
       const long long o = uf < 0.0 ? -s : s;  // stencil runs upwind
       const long long c0 = uf < 0.0 ? c + 3 * s : c - 2 * s;
       f1 = q[c0]; f2 = q[c0 + o]; f3 = q[c0 + 2 * o]; f4 = q[c0 + 3 * o]; f5 = q[c0 + 4 * o];
+      const double p1 = pr[c0], p2 = pr[c0 + o], p3 = pr[c0 + 2 * o], p4 = pr[c0 + 3 * o],
+                   p5 = pr[c0 + 4 * o];
       if (v == 2) {
-        f1 = f1 + pr[c0]; f2 = f2 + pr[c0 + o]; f3 = f3 + pr[c0 + 2 * o];
-        f4 = f4 + pr[c0 + 3 * o]; f5 = f5 + pr[c0 + 4 * o];
+        f1 = f1 + p1; f2 = f2 + p2; f3 = f3 + p3; f4 = f4 + p4; f5 = f5 + p5;
+      } else if (!(fst_finite(p1) && fst_finite(p2) && fst_finite(p3) && fst_finite(p4) &&
+                   fst_finite(p5))) {
+        // var + 0*p of the reference: NaN where a pressure is not finite
+        f1 = f1 + 0.0 * p1; f2 = f2 + 0.0 * p2; f3 = f3 + 0.0 * p3;
+        f4 = f4 + 0.0 * p4; f5 = f5 + 0.0 * p5;
       }
       Fd[sv * v + c] = dd(uf * weno2d(f1, f2, f3, f4, f5));
     }

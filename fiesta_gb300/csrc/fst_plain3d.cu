@@ -114,8 +114,10 @@ __device__ __forceinline__ double weno3d(double f1, double f2, double f3, double
 // on the x, y and z faces at (i+1/2, j, k), (i, j+1/2, k), (i, j, k+1/2),
 // face index box [ng-1, ngi-ng) in every dimension.
 // F layout: F[(dir*nv + v)*sv + cell].
-// The stencil value is var + (v==3)*p; for v != 3 that is var + 0*p, which is
-// var itself for every finite p (signed zeros aside), so only v == 3 adds p.
+// The stencil value is var + (v==3)*p.  For v != 3 that is var + 0*p: var
+// itself when the six pressures are finite (signed zeros aside, which never
+// change a nonzero result), and NaN otherwise; the add is only executed in
+// the second case, so NaN propagates exactly as in the reference.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_flux3d(Geo g, Phys P, const double* __restrict__ U,
                                                 const double* __restrict__ pr,
@@ -134,14 +136,20 @@ __global__ void __launch_bounds__(128) k_flux3d(Geo g, Phys P, const double* __r
     const double uf = (-vd[c + 2 * s] + 7.0f * vd[c + s] + 7.0f * vd[c] - vd[c - s]) / 12.0f;
     const DivC dd = dir == 0 ? P.ddx : dir == 1 ? P.ddy : P.ddz;
     double* Fd = F + (long long)dir * P.nv * sv;
+    const double p1 = pr[c + 3 * s], p2 = pr[c + 2 * s], p3 = pr[c + s], p4 = pr[c],
+                 p5 = pr[c - s], p6 = pr[c - 2 * s];
+    const bool pfin = fst_finite(p1) && fst_finite(p2) && fst_finite(p3) && fst_finite(p4) &&
+                      fst_finite(p5) && fst_finite(p6);
 #pragma unroll 1
     for (int v = 0; v < P.nv; ++v) {
       const double* q = U + sv * v;
       double f1 = q[c + 3 * s], f2 = q[c + 2 * s], f3 = q[c + s], f4 = q[c], f5 = q[c - s],
              f6 = q[c - 2 * s];
       if (v == 3) {
-        f1 = f1 + pr[c + 3 * s]; f2 = f2 + pr[c + 2 * s]; f3 = f3 + pr[c + s];
-        f4 = f4 + pr[c];         f5 = f5 + pr[c - s];     f6 = f6 + pr[c - 2 * s];
+        f1 = f1 + p1; f2 = f2 + p2; f3 = f3 + p3; f4 = f4 + p4; f5 = f5 + p5; f6 = f6 + p6;
+      } else if (!pfin) {
+        f1 = f1 + 0.0 * p1; f2 = f2 + 0.0 * p2; f3 = f3 + 0.0 * p3;
+        f4 = f4 + 0.0 * p4; f5 = f5 + 0.0 * p5; f6 = f6 + 0.0 * p6;
       }
       double wv = uf < 0.0 ? weno3d(f1, f2, f3, f4, f5) : weno3d(f6, f5, f4, f3, f2);
       Fd[sv * v + c] = dd(uf * wv);
@@ -378,6 +386,21 @@ __global__ void __launch_bounds__(128) k_cell3d(Geo g, Phys P, const double* __r
   emit(3, R3);
 }
 
+// Stage-1 ghost cells: U1 = U + (0.5*dt)*0 over ghosts (dvar is zero there;
+// src/rk.cpp:42-50 runs over every cell).  In 3D the next ghost fill
+// rewrites them, except where a periodic copy with fewer interior cells than
+// ghost layers reads ghosts; this keeps that case exact too.
+__global__ void k_ghost3d(Geo g, const double* __restrict__ Uold, double* __restrict__ Unew,
+                          double coef) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.sv) return;
+  int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj), k = (int)(c / g.sz);
+  bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng && k >= g.ng &&
+            k < g.ngk - g.ng;
+  if (in) return;
+  for (int v = 0; v < g.nvt; ++v) Unew[c + g.sv * v] = Uold[c + g.sv * v] + coef * 0.0;
+}
+
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 
 }  // namespace
@@ -385,7 +408,7 @@ inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 // One right-hand-side evaluation of Uin (ghosts already filled) followed by
 // the chosen output; returns the number of launches.
 int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* Uin,
-                      const double* Uold, double* Unew, double coef, double* Rout,
+                      const double* Uold, double* Unew, double coef, double* Rout, bool ghosts,
                       cudaStream_t st, Prof* prof) {
   int n = 0;
   if (P.ceq) {
@@ -408,6 +431,9 @@ int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const d
   FST_LAUNCH(prof, "cell3d", st, n,
              k_cell3d<<<gc, bf, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel, b.nrg, b.F, b.S, b.MF,
                                          b.red, Uold, Unew, coef, Rout));
+  if (ghosts && !Rout)
+    FST_LAUNCH(prof, "ghost3d", st, n,
+               k_ghost3d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, Uold, Unew, coef));
   return n;
 }
 

@@ -1,0 +1,121 @@
+"""Accuracy of the mixed-precision path (FP32 fluxes / viscous / C-equation,
+FP64 state, pressure recovery and RK combine) against the FP64 oracle.
+
+Tolerances (relative L2 per conserved field over the interior):
+  state after N steps          <= 1e-5   (the mixed-precision target)
+  state increment U_N - U_0    <= 2e-3   (the change the RHS produced)
+"""
+import numpy as np
+import pytest
+
+from fiesta_gb300 import abi
+from fiesta_gb300.solver import Solver, initial_conditions
+from oracle.oracle import Oracle
+from tests.golden_io import interior, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+STATE_TOL = 1e-5
+INCR_TOL = 2e-3
+
+SP5 = [dict(gamma=g, M=m / 1000.0, mu=mu) for g, m, mu in
+       zip([1.4, 1.67, 1.3, 1.32, 1.4], [28.96, 4.0, 44.0, 16.0, 2.0],
+           [1.8e-5, 1.99e-5, 1.47e-5, 1.1e-5, 0.88e-5])]
+
+
+def field_errors(cfg, U, Uref, U0):
+    nv = abi.nv_of(cfg)
+    out = []
+    for v in range(nv):
+        a, b, z = interior(cfg, U[..., v]), interior(cfg, Uref[..., v]), interior(cfg, U0[..., v])
+        st = rel_l2(a, b)
+        inc = rel_l2(a - z, b - z) if np.abs(b - z).max() > 0 else 0.0
+        out.append((v, st, inc))
+    return out
+
+
+def run_pair(cfg, U0, steps):
+    m = Solver(cfg)
+    m.set_state(U0)
+    m.rk_step(steps)
+    cref = abi.config_from_dict(abi.config_to_dict(cfg))
+    cref.mode = abi.MODE_PLAIN_FP64
+    o = Oracle(cref)
+    o.set_state(U0)
+    o.rk_step(steps)
+    return m.get_state(), o.get_state()
+
+
+def mixing(n, dt, mode=abi.MODE_MIXED):
+    return abi.make_config(3, n, dt=dt, species=SP5, visc=True, ceq=True, kap=10.0, eps=0.4,
+                           alpha=40.0, mode=mode)
+
+
+def test_mixed_mixing_3d_vs_oracle():
+    cfg = mixing((48, 40, 32), dt=2e-7)
+    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 20261206, p_ambient=1e5, T_ambient=300.0,
+                            nkernels=8)
+    U, Ur = run_pair(cfg, U0, 10)
+    for v, st, inc in field_errors(cfg, U, Ur, U0):
+        assert st <= STATE_TOL, (v, st)
+        assert inc <= INCR_TOL, (v, inc)
+
+
+def test_mixed_expansion_3d_vs_oracle():
+    cfg = abi.make_config(3, (32, 32, 32), dt=1e-6, species=SP5[:2], visc=True, ceq=True,
+                          mode=abi.MODE_MIXED)
+    U0 = initial_conditions(cfg, abi.IC_EXPANSION_3D, 20261204, p_ambient=1e5, T_ambient=300.0,
+                            p_high=1e7, radius=0.1 * 32 / 32, noise=0.01)
+    U, Ur = run_pair(cfg, U0, 10)
+    for v, st, inc in field_errors(cfg, U, Ur, U0):
+        assert st <= STATE_TOL, (v, st)
+        assert inc <= INCR_TOL, (v, inc)
+
+
+@pytest.mark.parametrize("case", ["sod", "rt"])
+def test_mixed_2d_vs_oracle(case):
+    if case == "sod":
+        cfg = abi.make_config(2, (100, 40), dt=1e-4, species=[dict(gamma=1.4, M=1.0, mu=0.0)],
+                              R=1.0, ceq=True, bcs=("outflow", "outflow", "reflective",
+                                                    "reflective", "outflow", "outflow"),
+                              mode=abi.MODE_MIXED)
+        U0 = initial_conditions(cfg, abi.IC_SHOCK_TUBE_2D, 1)
+    else:
+        cfg = abi.make_config(2, (48, 96), L=(1.0 / 3.0, 1.0), dt=1e-4,
+                              species=[dict(gamma=1.4, M=1.0, mu=0.0), dict(gamma=1.4, M=2.0, mu=0.0)],
+                              R=1.0, visc=True, ceq=True, buoyancy=True, g=0.5, rho_ref=1.5,
+                              periodic=(True, False, False),
+                              bcs=("outflow", "outflow", "hydrostatic", "hydrostatic", "outflow",
+                                   "outflow"), mode=abi.MODE_MIXED)
+        U0 = initial_conditions(cfg, abi.IC_RT_2D, 7, rho_heavy=2.0, rho_light=1.0, p_ambient=2.4)
+    U, Ur = run_pair(cfg, U0, 50)
+    for v, st, inc in field_errors(cfg, U, Ur, U0):
+        assert st <= STATE_TOL, (v, st)
+        assert inc <= INCR_TOL, (v, inc)
+
+
+def test_mixed_rhs_close_to_oracle():
+    cfg = mixing((24, 20, 16), dt=2e-7)
+    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 5, p_ambient=1e5, T_ambient=300.0, nkernels=8)
+    m = Solver(cfg)
+    m.set_state(U0)
+    R = m.compute_rhs()
+    cref = abi.config_from_dict(abi.config_to_dict(cfg))
+    cref.mode = abi.MODE_PLAIN_FP64
+    o = Oracle(cref)
+    o.set_state(U0)
+    Ro = o.compute_rhs()
+    for v in range(abi.dims(cfg)[3]):
+        e = rel_l2(interior(cfg, R[..., v]), interior(cfg, Ro[..., v]))
+        assert e <= 1e-3, (v, e)
+
+
+def test_mixed_many_species_fallback():
+    # 7 species takes the generic (predicated) kernel instance
+    sp = [dict(gamma=1.3 + 0.05 * s, M=0.5 + 0.3 * s, mu=1e-3) for s in range(7)]
+    cfg = abi.make_config(3, (12, 10, 9), dt=1e-4, species=sp, R=1.0, visc=True, ceq=True,
+                          mode=abi.MODE_MIXED)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 3)
+    U, Ur = run_pair(cfg, U0, 5)
+    for v, st, inc in field_errors(cfg, U, Ur, U0):
+        assert st <= STATE_TOL, (v, st)

@@ -118,3 +118,19 @@ def test_gpu_full_size_periodic_conservation():
         m0 = interior(cfg, U0[..., 4 + s]).sum()
         m1 = interior(cfg, U[..., 4 + s]).sum()
         assert abs(m1 - m0) <= 1e-11 * abs(m0), (s, m0, m1)
+
+
+@pytest.mark.parametrize("n", [(1, 5, 4), (2, 1, 3), (5, 2, 1)])
+def test_gpu_degenerate_periodic(n):
+    sp = [dict(gamma=1.4, M=1.0, mu=1e-3), dict(gamma=1.6, M=2.0, mu=2e-3)]
+    cfg = abi.make_config(3, n, dt=1e-3, species=sp, R=1.0, visc=True, ceq=True,
+                          periodic=(True, True, True))
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 4)
+    o, g = Oracle(cfg), Solver(cfg)
+    for x in (o, g):
+        x.set_state(U0)
+        x.apply_bcs()
+    assert same(g.compute_rhs(), o.compute_rhs())
+    o.rk_step(2)
+    g.rk_step(2)
+    assert same(g.get_state(), o.get_state())
