@@ -139,6 +139,9 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
   P.d12y = 12.0 * P.dy;
   P.d12z = 12.0 * P.dz;
   P.d12pz = 12.0 * P.dy;
+  P.r12x = 1.0 / P.d12x;
+  P.r12y = 1.0 / P.d12y;
+  P.r12pz = 1.0 / P.d12pz;
   P.dt = cf.dt;
   P.hdt = 0.5f * cf.dt;
   P.kap = cf.kap;

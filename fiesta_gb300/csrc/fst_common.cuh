@@ -43,6 +43,7 @@ struct Phys {
   DivC d4x, d4y, d4z;     // x/(4*dx) ... (viscous and C-equation tangential terms)
   double d12x, d12y, d12z;  // 12.0*dx, 12.0*dy, 12.0*dz (4th-order derivatives)
   double d12pz;           // 12.0*cd(2): the reference's dz = cd(2) in presgrad3D
+  double r12x, r12y, r12pz;  // their reciprocals (mixed path)
   double dt, hdt;         // dt and 0.5f*dt
   double kap, eps, alpha, g, rho_ref;
   double dxmag2;          // dx^2+dy^2(+dz^2): alpha numerator

@@ -87,7 +87,8 @@ int fst_plain2d_secondary(const Geo& g, const Phys& P, const Plain2DBufs& b, con
 struct MixedBufs {
   // FP32 primitives written by the mixed primitive pass
   float *Q, *rho32, *vel32, *Y, *T32, *nrg, *C;
-  double* p64;  // FP64 pressure
+  double* p64;    // FP64 pressure
+  double* rho64;  // FP64 density (buoyancy source)
   // FP64 secondary outputs (fst_secondary)
   double *rho, *pr, *vel, *T;
   unsigned long long* red;
@@ -106,6 +107,7 @@ struct MixedView {
   const float* nrg;  // [cells]
   const float* C;    // [5][cells]
   const float* T;    // [cells] (2D viscous heat flux)
+  const double* rho64;  // [cells] FP64 density (buoyancy)
 };
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);

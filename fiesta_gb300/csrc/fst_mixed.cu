@@ -3,11 +3,12 @@
 // (FST_MODE_HYBRID) for sm_103a.
 //
 // Precision split:
-//   FP64  the conserved state, the RK stage combine, the pressure recovery
-//         p = (gamma-1)*(E - KE) (the low-Mach cancellation), the stored
-//         pressure and its 4th-order gradient, E + p
-//   FP32  mixture properties from FP32 mass fractions, velocities, WENO5
-//         reconstruction and fluxes, viscous stress, C-equation terms
+//   FP64  the conserved state, the RK stage combine, the equation of state
+//         (rho, mass fractions, gamma, p = (gamma-1)*(E - KE): the low-Mach
+//         cancellation), the stored pressure and its 4th-order gradient,
+//         E + p, and the buoyancy source
+//   FP32  velocities, WENO5 reconstruction and fluxes, viscous stress,
+//         C-equation terms, the wave-speed and C_hat maxima
 //
 // Two kernels per stage:
 //   k_mprim    all cells: FP64 state -> FP32 primitives (+ FP64 p), and the
@@ -42,81 +43,100 @@ constexpr int NVMAX = 4 + FST_MAX_SPECIES;
 // ---------------------------------------------------------------------------
 // primitives
 // ---------------------------------------------------------------------------
+// FP64 reciprocal by two Newton-Raphson steps from an FP32 seed (relative
+// error ~1e-16 for arguments inside the FP32 range, which holds for the
+// densities and heat capacities it is used on).
+__device__ __forceinline__ double rcp64(double x) {
+  double r = (double)__frcp_rn((float)x);
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
 template <int NDIM>
 __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __restrict__ U,
                                                float* __restrict__ Q, float* __restrict__ rho,
+                                               double* __restrict__ rho64,
                                                float* __restrict__ vel, double* __restrict__ pr,
                                                float* __restrict__ Y, float* __restrict__ nrg,
                                                float* __restrict__ Cc, float* __restrict__ T,
                                                unsigned long long* __restrict__ red) {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // grid: x covers i in blocks of 256, y = j, z = k (no integer division)
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, k = blockIdx.z;
   const long long sv = g.sv;
-  float lS = -3.0e38f;
-  double lC = -1.7976931348623157e308;
-  if (c < sv) {
+  float lS = -3.0e38f, lC = -3.0e38f;
+  if (i < g.ngi) {
+    const long long c = (long long)i + g.sy * j + g.sz * k;
     const int s0 = NDIM + 1;  // first species index
-    float r = 0.f;
-    for (int s = 0; s < P.ns; ++s) r += (float)U[c + sv * (s0 + s)];
-    const float ri = 1.0f / r;
-    float Cv = 0.f, Rm = 0.f, Cv2 = 0.f, Cp2 = 0.f;
+    // mixture EOS in FP64 (calculateRhoPT, src/secondary.hpp:60-151)
+    double r = 0.0;
+    for (int s = 0; s < P.ns; ++s) r += U[c + sv * (s0 + s)];
+    const double ri = rcp64(r);
+    double Cv = 0.0, Rm = 0.0;
+    float Cv2 = 0.f, Cp2 = 0.f;
     for (int s = 0; s < P.ns; ++s) {
-      const float rs = (float)U[c + sv * (s0 + s)];
-      const float ys = rs * ri;
-      Cv += ys * P.cv_f[s];
-      Rm += ys * P.rm_f[s];
+      const double rs = U[c + sv * (s0 + s)];
+      const double ys = rs * ri;
+      Cv = fma(ys, P.cv_s[s], Cv);
+      Rm = fma(ys, P.cp_s[s] - P.cv_s[s], Rm);
       if (NDIM == 2) {
-        Cv2 += ys * P.cv2_f[s];
-        Cp2 += ys * P.cp2_f[s];
+        Cv2 += (float)ys * P.cv2_f[s];
+        Cp2 += (float)ys * P.cp2_f[s];
       }
-      if (Y) Y[c + sv * s] = ys;
-      Q[c + sv * (s0 + s)] = rs;
+      if (Y) Y[c + sv * s] = (float)ys;
+      Q[c + sv * (s0 + s)] = (float)rs;
     }
-    const float gm1 = Rm / Cv;  // gamma - 1 of the mixture
-    float usq = 0.f, msq = 0.f;
+    const double gm1 = Rm * rcp64(Cv);  // gamma - 1 of the mixture
+    double msq = 0.0;
+    float usq = 0.f;
+    const float rif = (float)ri;
 #pragma unroll
     for (int d = 0; d < NDIM; ++d) {
-      const float m = (float)U[c + sv * d];
-      const float u = m * ri;
+      const double m = U[c + sv * d];
+      msq = fma(m, m, msq);
+      const float u = (float)m * rif;
       usq += u * u;
-      msq += m * m;
       vel[c + sv * d] = u;
-      Q[c + sv * d] = m;
+      Q[c + sv * d] = (float)m;
     }
     const double E = U[c + sv * NDIM];
-    const float ke = 0.5f * msq * ri;
-    const double p = (double)gm1 * (E - (double)ke);  // FP64 pressure recovery
+    const double p = gm1 * (E - 0.5 * msq * ri);  // FP64 pressure recovery
     pr[c] = p;
     Q[c + sv * NDIM] = (float)(E + p);
-    rho[c] = r;
-    if (T) T[c] = (float)p * ri / Rm;
-    if (nrg) nrg[c] = (float)E * ri - 0.5f * r * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
+    const float rf = (float)r;
+    rho[c] = rf;
+    if (rho64) rho64[c] = r;
+    if (T) T[c] = (float)(p * ri / Rm);
+    if (nrg) nrg[c] = (float)E * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
     if (Cc)
       for (int n = 0; n < 5; ++n) Cc[c + sv * n] = (float)U[c + sv * (P.nv + n)];
     if (red) {
-      const int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj);
-      const int k = NDIM == 3 ? (int)(c / g.sz) : g.ng;
       const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
                       (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
       if (in) {
+        const float pf = (float)p, mf = sqrtf((float)msq);
         float s;
-        if (NDIM == 3) {
-          s = sqrtf((1.0f + gm1) * (float)p * ri) + sqrtf(msq) * ri;
-        } else {
-          // maxWaveSpeed2D: stride-2 species table, momentum without /rho
-          s = sqrtf(Cp2 / Cv2 * (float)p * ri) + sqrtf(msq);
-        }
-        if (s > lS) lS = s;
-        const double ch = fabs(U[c + sv * (P.nv + 1)]);
-        if (ch > lC) lC = ch;
+        if (NDIM == 3) s = sqrtf((1.0f + (float)gm1) * pf * rif) + mf * rif;
+        else s = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
+        lS = fmaxf(lS, s);
+        lC = fmaxf(lC, fabsf(Cc[c + sv]));
       }
     }
   }
   if (red) {
-    const double ds = fst_warp_max((double)lS);
-    lC = fst_warp_max(lC);
-    if ((threadIdx.x & 31) == 0) {
-      if (ds > -1e38) atomicMax(&red[0], fst_key(ds));
-      atomicMax(&red[1], fst_key(lC));
+    lS = warp_maxf(lS);
+    lC = warp_maxf(lC);
+    if ((threadIdx.x & 31) == 0 && lS > -1e38f) {
+      atomicMax(&red[0], fst_key((double)lS));
+      atomicMax(&red[1], fst_key((double)lC));
     }
   }
 }
@@ -314,14 +334,14 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
     if (cell_col) {
       // pressure gradient in FP64 (reference quirk: z spacing is dy)
       const double* p = M.p;
-      const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) / P.d12x;
-      const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) / P.d12y;
-      const double dpz = (p[c - 2 * sz] - 8.0 * p[c - sz] + 8.0 * p[c + sz] - p[c + 2 * sz]) / P.d12pz;
+      const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) * P.r12x;
+      const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) * P.r12y;
+      const double dpz = (p[c - 2 * sz] - 8.0 * p[c - sz] + 8.0 * p[c + sz] - p[c + 2 * sz]) * P.r12pz;
       double Rd[4] = {(double)R[0] - dpx, (double)R[1] - dpy, (double)R[2] - dpz, (double)R[3]};
       if (P.buoyancy) {
-        const float f = -(float)P.g * (M.rho[c] - (float)P.rho_ref);
+        const double f = -P.g * (M.rho64[c] - P.rho_ref);
         Rd[1] += f;
-        Rd[3] += (double)(M.vel[c + sv] * f);
+        Rd[3] += (double)M.vel[c + sv] * f;
       }
       auto emit = [&](int v, double Rv) {
         if (Rout) Rout[c + sv * v] = Rv;
@@ -483,16 +503,16 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
   }
   if (!(ci && cj)) return;
   const double* p = M.p;
-  const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) / P.d12x;
-  const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) / P.d12y;
+  const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) * P.r12x;
+  const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) * P.r12y;
   double Rd[3] = {(double)R[0] - dpx, (double)R[1] - dpy, (double)R[2]};
   if (P.buoyancy) {
-    const float rhop = M.rho[c] - (float)P.rho_ref;
-    if (rhop >= 1e-6f || rhop <= -1e-6f) {
-      const float f = -(float)P.g * rhop;
+    const double rhop = M.rho64[c] - P.rho_ref;
+    if (rhop >= 1e-6 || rhop <= -1e-6) {
+      const double f = -P.g * rhop;
       const float vb = M.Q[c + sv] / M.Q[c + 3 * sv];  // m_y / rho_1 (reference)
       Rd[1] += f;
-      Rd[2] += (double)(fabsf(vb) * f);
+      Rd[2] += (double)fabsf(vb) * f;
     }
   }
   auto emit = [&](int v, double Rv) {
@@ -535,10 +555,10 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
 
 // ghost cells of the stage-1 buffer: U1 = U + (0.5*dt)*0 (src/rk.cpp:42-50)
 __global__ void k_mghost(Geo g, const double* __restrict__ Uold, double* __restrict__ Unew) {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.sv) return;
-  const int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj);
-  const int k = g.ndim == 3 ? (int)(c / g.sz) : g.ng;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, k = g.ndim == 3 ? (int)blockIdx.z : g.ng;
+  if (i >= g.ngi) return;
+  const long long c = (long long)i + g.sy * j + g.sz * blockIdx.z;
   const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
                   (g.ndim == 2 || (k >= g.ng && k < g.ngk - g.ng));
   if (in) return;
@@ -597,6 +617,7 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   A((void**)&b.rho32, sizeof(float) * n);
   A((void**)&b.vel32, sizeof(float) * n * g.ndim);
   A((void**)&b.p64, sizeof(double) * n);
+  if (cf.buoyancy) A((void**)&b.rho64, sizeof(double) * n);
   if (cf.visc && g.ndim == 3) A((void**)&b.Y, sizeof(float) * n * g.ns);
   if (cf.visc && g.ndim == 2) A((void**)&b.T32, sizeof(float) * n);
   if (cf.ceq) {
@@ -621,18 +642,20 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const Mix
     const unsigned long long init[2] = {FST_KEY_LOWEST, FST_KEY_LOWEST};
     cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
   }
-  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.Y, b.nrg, b.C, b.T32};
+  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.Y, b.nrg, b.C, b.T32, b.rho64};
+  const dim3 pg(cdiv(g.ngi, 256), g.ngj, g.ngk);
   if (g.ndim == 3) {
     FST_LAUNCH(prof, "mprim3d", st, n,
-               k_mprim<3><<<cdiv(g.sv, 256), 256, 0, st>>>(
-                   g, P, Uin, b.Q, b.rho32, b.vel32, b.p64, P.visc ? b.Y : nullptr,
+               k_mprim<3><<<pg, 256, 0, st>>>(
+                   g, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, P.visc ? b.Y : nullptr,
                    P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, nullptr,
                    P.ceq ? b.red : nullptr));
   } else {
     FST_LAUNCH(prof, "mprim2d", st, n,
-               k_mprim<2><<<cdiv(g.sv, 256), 256, 0, st>>>(
-                   g, P, Uin, b.Q, b.rho32, b.vel32, b.p64, nullptr, P.ceq ? b.nrg : nullptr,
-                   P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr, P.ceq ? b.red : nullptr));
+               k_mprim<2><<<pg, 256, 0, st>>>(
+                   g, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
+                   P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr,
+                   P.ceq ? b.red : nullptr));
   }
   const bool hyb = cf.mode == FST_MODE_HYBRID && b.hyb_active;
   const unsigned char* smooth = nullptr;
@@ -644,7 +667,7 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const Mix
     FST_LAUNCH(prof, g.ndim == 3 ? "mrhs3d" : "mrhs2d", st, n,
                dispatch_rhs<false>(g, P, M, b.red, nullptr, Uold, Unew, coef, Rout, st));
   if (ghosts && !Rout)
-    FST_LAUNCH(prof, "mghost", st, n, k_mghost<<<cdiv(g.sv, 256), 256, 0, st>>>(g, Uold, Unew));
+    FST_LAUNCH(prof, "mghost", st, n, k_mghost<<<pg, 256, 0, st>>>(g, Uold, Unew));
   return n;
 }
 

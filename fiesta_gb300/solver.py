@@ -54,14 +54,21 @@ _EXPORTS = {
 
 
 def lib():
-    """Load fiesta_gb300/libfst.so (building it first if sources are newer)."""
+    """Load fiesta_gb300/libfst.so (building it first if sources are newer).
+
+    FST_LIB names another build of the same library to load instead (for
+    A/B timing of build variants); no build check is made for it.
+    """
     global _lib
     if _lib is None:
-        if not up_to_date():
-            build()
-        if not os.path.exists(LIB):
-            raise RuntimeError(f"libfst.so not found at {LIB}; run __graft_entry__.build()")
-        L = C.CDLL(LIB)
+        path = os.environ.get("FST_LIB")
+        if not path:
+            path = LIB
+            if not up_to_date():
+                build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libfst.so not found at {path}; run __graft_entry__.build()")
+        L = C.CDLL(path)
         for name, (res, args) in _EXPORTS.items():
             fn = getattr(L, name)
             fn.restype = res
