@@ -158,6 +158,19 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
   }
   P.mu2d = 2.928e-5;
   P.kheat2d = 0.026;
+  P.rd_f[0] = (float)(1.0 / P.dx);
+  P.rd_f[1] = (float)(1.0 / P.dy);
+  P.rd_f[2] = (float)(1.0 / P.dz);
+  P.r12_f[0] = (float)(1.0 / P.d12x);
+  P.r12_f[1] = (float)(1.0 / P.d12y);
+  P.r12_f[2] = (float)(1.0 / P.d12z);
+  P.dxmag_f = (float)P.dxmag;
+  P.dxmag2_f = (float)P.dxmag2;
+  P.eps_f = (float)P.eps;
+  P.kap_f = (float)P.kap;
+  P.alpha_f = (float)P.alpha;
+  P.mu2d_f = (float)P.mu2d;
+  P.kheat_f = (float)P.kheat2d;
   for (int s = 0; s < g.ns; ++s) {
     P.cv_f[s] = (float)P.cv_s[s];
     P.rm_f[s] = (float)(P.cp_s[s] - P.cv_s[s]);

@@ -54,6 +54,10 @@ struct Phys {
   // stride-2 table constants
   float cv_f[FST_MAX_SPECIES], rm_f[FST_MAX_SPECIES], mu_f[FST_MAX_SPECIES];
   float cv2_f[FST_MAX_SPECIES], cp2_f[FST_MAX_SPECIES];
+  // FP32 copies of the grid constants (mixed path)
+  float rd_f[3];    // 1/dx, 1/dy, 1/dz
+  float r12_f[3];   // 1/(12 dx), 1/(12 dy), 1/(12 dz)
+  float dxmag_f, dxmag2_f, eps_f, kap_f, alpha_f, mu2d_f, kheat_f;
 };
 
 // --- order-preserving encoding of doubles for atomicMax -------------------

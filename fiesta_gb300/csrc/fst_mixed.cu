@@ -43,11 +43,37 @@ constexpr int NVMAX = 4 + FST_MAX_SPECIES;
 // ---------------------------------------------------------------------------
 // primitives
 // ---------------------------------------------------------------------------
+// FP64 <-> FP32 conversions on the integer pipe.  GB300's FP64 unit also
+// executes the F2F conversions, at the FP64 rate; these rebias the exponent
+// and round the mantissa with integer operations instead.  Values outside
+// the FP32 normal range go to signed zero / infinity (no FP32 denormals);
+// NaN stays NaN; mantissa ties round away from zero.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+  const unsigned int sign = hi & 0x80000000u;
+  const unsigned int ex = (hi >> 20) & 0x7FFu;
+  const int e = (int)ex - 1023 + 127;
+  const unsigned int m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  const unsigned int r = (lo >> 28) & 1u;
+  unsigned int bits = (((unsigned int)e << 23) | m) + r;  // a carry rounds into the exponent
+  if (e <= 0) bits = 0u;
+  if (e >= 255) bits = (ex == 0x7FFu && ((hi & 0xFFFFFu) | lo)) ? 0x7FC00000u : 0x7F800000u;
+  return __uint_as_float(sign | bits);
+}
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned int f = __float_as_uint(x);
+  const unsigned int sign = f & 0x80000000u, e = (f >> 23) & 0xFFu, m = f & 0x7FFFFFu;
+  unsigned int hi = sign | ((e + 896u) << 20) | (m >> 3);
+  if (e == 0u) hi = sign;                                   // zero (and FP32 denormals)
+  if (e == 255u) hi = sign | 0x7FF00000u | (m >> 3) | (m ? 0x80000u : 0u);  // inf / NaN
+  return __hiloint2double((int)hi, e == 0u ? 0 : (int)(m << 29));
+}
+
 // FP64 reciprocal by two Newton-Raphson steps from an FP32 seed (relative
 // error ~1e-16 for arguments inside the FP32 range, which holds for the
 // densities and heat capacities it is used on).
 __device__ __forceinline__ double rcp64(double x) {
-  double r = (double)__frcp_rn((float)x);
+  double r = f2d(__frcp_rn(d2f(x)));
   double e = fma(-x, r, 1.0);
   r = fma(r, e, r);
   e = fma(-x, r, 1.0);
@@ -76,55 +102,59 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __re
   if (i < g.ngi) {
     const long long c = (long long)i + g.sy * j + g.sz * k;
     const int s0 = NDIM + 1;  // first species index
-    // mixture EOS in FP64 (calculateRhoPT, src/secondary.hpp:60-151)
-    double r = 0.0;
-    for (int s = 0; s < P.ns; ++s) r += U[c + sv * (s0 + s)];
-    const double ri = rcp64(r);
-    double Cv = 0.0, Rm = 0.0;
-    float Cv2 = 0.f, Cp2 = 0.f;
+    // mixture EOS in FP64 (calculateRhoPT, src/secondary.hpp:60-151):
+    // gamma - 1 = R_mix / Cv = (sum rho_s R_s) / (sum rho_s cv_s)
+    double r = 0.0, sCv = 0.0, sRm = 0.0;
     for (int s = 0; s < P.ns; ++s) {
       const double rs = U[c + sv * (s0 + s)];
-      const double ys = rs * ri;
-      Cv = fma(ys, P.cv_s[s], Cv);
-      Rm = fma(ys, P.cp_s[s] - P.cv_s[s], Rm);
-      if (NDIM == 2) {
-        Cv2 += (float)ys * P.cv2_f[s];
-        Cp2 += (float)ys * P.cp2_f[s];
-      }
-      if (Y) Y[c + sv * s] = (float)ys;
-      Q[c + sv * (s0 + s)] = (float)rs;
+      r += rs;
+      sCv = fma(rs, P.cv_s[s], sCv);
+      sRm = fma(rs, P.cp_s[s] - P.cv_s[s], sRm);
     }
-    const double gm1 = Rm * rcp64(Cv);  // gamma - 1 of the mixture
+    const double ri = rcp64(r);
+    const double gm1 = sRm * rcp64(sCv);
+    const float rif = d2f(ri);
+    float Cv2 = 0.f, Cp2 = 0.f;
+    for (int s = 0; s < P.ns; ++s) {
+      const float rs = d2f(U[c + sv * (s0 + s)]);
+      const float ys = rs * rif;
+      if (NDIM == 2) {
+        Cv2 += ys * P.cv2_f[s];
+        Cp2 += ys * P.cp2_f[s];
+      }
+      if (Y) Y[c + sv * s] = ys;
+      Q[c + sv * (s0 + s)] = rs;
+    }
     double msq = 0.0;
     float usq = 0.f;
-    const float rif = (float)ri;
 #pragma unroll
     for (int d = 0; d < NDIM; ++d) {
       const double m = U[c + sv * d];
       msq = fma(m, m, msq);
-      const float u = (float)m * rif;
+      const float mf = d2f(m);
+      const float u = mf * rif;
       usq += u * u;
       vel[c + sv * d] = u;
-      Q[c + sv * d] = (float)m;
+      Q[c + sv * d] = mf;
     }
     const double E = U[c + sv * NDIM];
     const double p = gm1 * (E - 0.5 * msq * ri);  // FP64 pressure recovery
     pr[c] = p;
-    Q[c + sv * NDIM] = (float)(E + p);
-    const float rf = (float)r;
+    Q[c + sv * NDIM] = d2f(E + p);
+    const float rf = d2f(r);
     rho[c] = rf;
     if (rho64) rho64[c] = r;
-    if (T) T[c] = (float)(p * ri / Rm);
-    if (nrg) nrg[c] = (float)E * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
+    if (T) T[c] = d2f(p) * rif / d2f(sRm * ri);
+    if (nrg) nrg[c] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
     if (Cc)
-      for (int n = 0; n < 5; ++n) Cc[c + sv * n] = (float)U[c + sv * (P.nv + n)];
+      for (int n = 0; n < 5; ++n) Cc[c + sv * n] = d2f(U[c + sv * (P.nv + n)]);
     if (red) {
       const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
                       (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
       if (in) {
-        const float pf = (float)p, mf = sqrtf((float)msq);
+        const float pf = d2f(p), mf = sqrtf(d2f(msq));
         float s;
-        if (NDIM == 3) s = sqrtf((1.0f + (float)gm1) * pf * rif) + mf * rif;
+        if (NDIM == 3) s = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
         else s = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
         lS = fmaxf(lS, s);
         lC = fmaxf(lC, fabsf(Cc[c + sv]));
@@ -182,18 +212,17 @@ struct FaceCtx {
 __device__ __forceinline__ FaceCtx make_ctx(const Phys& P, const unsigned long long* red,
                                             float* maxS) {
   FaceCtx fc;
-  fc.rd[0] = (float)(1.0 / P.dx);
-  fc.rd[1] = (float)(1.0 / P.dy);
-  fc.rd[2] = (float)(1.0 / P.dz);
-  fc.r4d[0] = 0.25f * fc.rd[0];
-  fc.r4d[1] = 0.25f * fc.rd[1];
-  fc.r4d[2] = 0.25f * fc.rd[2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    fc.rd[d] = P.rd_f[d];
+    fc.r4d[d] = 0.25f * P.rd_f[d];
+  }
   fc.alpha = 0.f;
   *maxS = 0.f;
   if (P.ceq) {
-    const double maxCh = fst_unkey(red[1]);
-    fc.alpha = (float)((P.dxmag2 / (maxCh + 1.0e-6)) * P.alpha);  // src/cart3d.cpp:285
-    *maxS = (float)fst_unkey(red[0]);
+    const float maxCh = d2f(fst_unkey(red[1]));
+    fc.alpha = P.dxmag2_f / (maxCh + 1.0e-6f) * P.alpha_f;  // src/cart3d.cpp:285
+    *maxS = d2f(fst_unkey(red[0]));
   }
   return fc;
 }
@@ -337,11 +366,11 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
       const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) * P.r12x;
       const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) * P.r12y;
       const double dpz = (p[c - 2 * sz] - 8.0 * p[c - sz] + 8.0 * p[c + sz] - p[c + 2 * sz]) * P.r12pz;
-      double Rd[4] = {(double)R[0] - dpx, (double)R[1] - dpy, (double)R[2] - dpz, (double)R[3]};
+      double Rd[4] = {f2d(R[0]) - dpx, f2d(R[1]) - dpy, f2d(R[2]) - dpz, f2d(R[3])};
       if (P.buoyancy) {
         const double f = -P.g * (M.rho64[c] - P.rho_ref);
         Rd[1] += f;
-        Rd[3] += (double)M.vel[c + sv] * f;
+        Rd[3] += f2d(M.vel[c + sv]) * f;
       }
       auto emit = [&](int v, double Rv) {
         if (Rout) Rout[c + sv * v] = Rv;
@@ -352,11 +381,10 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
 #pragma unroll
       for (int v = 4; v < NV; ++v) {
         if (NV == NVMAX && v >= nv) break;
-        emit(v, (double)R[v]);
+        emit(v, f2d(R[v]));
       }
       if (P.ceq) {
-        const float r12x = (float)(1.0 / P.d12x), r12y = (float)(1.0 / P.d12y),
-                    r12z = (float)(1.0 / P.d12z);
+        const float r12x = P.r12_f[0], r12y = P.r12_f[1], r12z = P.r12_f[2];
         auto d4 = [&](const float* a, long long st, float r12) {
           return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
         };
@@ -367,9 +395,9 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
         const float dnednr = (dxr * dxe + dyr * dye + dzr * dze) * (dxr * dxr + dyr * dyr + dzr * dzr);
         const bool ind = dnednr < 0.0f;
         const float Gs[5] = {divu < 0.f && !ind ? rgrad : 0.f, ind ? rgrad : 0.f, dxr, dyr, dzr};
-        const float dxm = (float)P.dxmag;
-        const float src = maxS / ((float)P.eps * dxm);
-        const float dif = (float)P.kap * maxS * dxm;
+        const float dxm = P.dxmag_f;
+        const float src = maxS / (P.eps_f * dxm);
+        const float dif = P.kap_f * maxS * dxm;
 #pragma unroll
         for (int n = 0; n < 5; ++n) {
           const float* Cn = M.C + sv * n;
@@ -377,7 +405,7 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
           const float lap = (Cn[c - 1] - 2.0f * cc + Cn[c + 1]) * fc.rd[0] +
                             (Cn[c - sy] - 2.0f * cc + Cn[c + sy]) * fc.rd[1] +
                             (Cn[c - sz] - 2.0f * cc + Cn[c + sz]) * fc.rd[2];
-          emit(nv + n, (double)(src * (Gs[n] - cc) + dif * lap));
+          emit(nv + n, f2d(src * (Gs[n] - cc) + dif * lap));
         }
       }
     }
@@ -416,7 +444,7 @@ __device__ __forceinline__ void face2d(const Geo& g, const Phys& P, const MixedV
   const float* v = M.vel + sv;
   float V[3] = {0.f, 0.f, 0.f};  // x-, y-momentum, energy
   if (P.visc) {
-    const float mu = (float)P.mu2d;
+    const float mu = P.mu2d_f;
     float dudx, dvdx, dudy, dvdy;
     if (f == 0) {
       dudx = (u[c + sx] - u[c]) * fc.rd[0];
@@ -434,7 +462,7 @@ __device__ __forceinline__ void face2d(const Geo& g, const Phys& P, const MixedV
     const float sxy = mu * (dudy + dvdx);
     const float sn = f == 0 ? sxx : sxy;  // x-momentum component on this face
     const float st = f == 0 ? sxy : syy;  // y-momentum component
-    const float q = -(float)P.kheat2d * (M.T[c + sf] - M.T[c]) * fc.rd[f];
+    const float q = -P.kheat_f * (M.T[c + sf] - M.T[c]) * fc.rd[f];
     V[0] = sn;
     V[1] = st;
     V[2] = 0.5f * (u[c + sf] + u[c]) * sn + 0.5f * (v[c + sf] + v[c]) * st - q;
@@ -505,14 +533,14 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
   const double* p = M.p;
   const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) * P.r12x;
   const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) * P.r12y;
-  double Rd[3] = {(double)R[0] - dpx, (double)R[1] - dpy, (double)R[2]};
+  double Rd[3] = {f2d(R[0]) - dpx, f2d(R[1]) - dpy, f2d(R[2])};
   if (P.buoyancy) {
     const double rhop = M.rho64[c] - P.rho_ref;
     if (rhop >= 1e-6 || rhop <= -1e-6) {
       const double f = -P.g * rhop;
       const float vb = M.Q[c + sv] / M.Q[c + 3 * sv];  // m_y / rho_1 (reference)
       Rd[1] += f;
-      Rd[2] += (double)fabsf(vb) * f;
+      Rd[2] += f2d(fabsf(vb)) * f;
     }
   }
   auto emit = [&](int v, double Rv) {
@@ -524,10 +552,10 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
 #pragma unroll
   for (int v = 3; v < NV; ++v) {
     if (NV == NVMAX && v >= nv) break;
-    emit(v, (double)R[v]);
+    emit(v, f2d(R[v]));
   }
   if (P.ceq) {
-    const float r12x = (float)(1.0 / P.d12x), r12y = (float)(1.0 / P.d12y);
+    const float r12x = P.r12_f[0], r12y = P.r12_f[1];
     auto d4 = [&](const float* a, long long st, float r12) {
       return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
     };
@@ -538,16 +566,16 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
     const float dnednr = (dxr * dxe + dyr * dye) * (dxr * dxr + dyr * dyr);
     const bool i1 = dnednr < 0.0f;
     const float Gs[4] = {(!i1 && divu < 0.f) ? rgrad : 0.f, i1 ? rgrad : 0.f, -dyr, dxr};
-    const float dxm = (float)P.dxmag;
-    const float src = maxS / ((float)P.eps * dxm);
-    const float dif = (float)P.kap * maxS * dxm;
+    const float dxm = P.dxmag_f;
+    const float src = maxS / (P.eps_f * dxm);
+    const float dif = P.kap_f * maxS * dxm;
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
       const float* Cn = M.C + sv * n;
       const float cc = Cn[c];
       const float lap = (Cn[c + 1] - 2.0f * cc + Cn[c - 1]) * fc.rd[0] +
                         (Cn[c + sy] - 2.0f * cc + Cn[c - sy]) * fc.rd[1];
-      emit(nv + n, (double)(src * (Gs[n] - cc) + dif * lap));
+      emit(nv + n, f2d(src * (Gs[n] - cc) + dif * lap));
     }
     emit(nv + 4, 0.0);
   }

@@ -2,8 +2,12 @@
 FP64 state, pressure recovery and RK combine) against the FP64 oracle.
 
 Tolerances (relative L2 per conserved field over the interior):
-  state after N steps          <= 1e-5   (the mixed-precision target)
-  state increment U_N - U_0    <= 2e-3   (the change the RHS produced)
+  state after N steps          <= 1e-5   (the mixed-precision target), for
+                                         fields that are not zero initially
+  state increment U_N - U_0    <= 2e-3   (the change the RHS produced), for
+                                         every field; for a field that starts
+                                         at zero (momenta at rest, C
+                                         variables) this is its whole value
 """
 import numpy as np
 import pytest
@@ -24,11 +28,12 @@ SP5 = [dict(gamma=g, M=m / 1000.0, mu=mu) for g, m, mu in
 
 
 def field_errors(cfg, U, Uref, U0):
+    """(v, state error or 0 for zero-initial fields, increment error)."""
     nv = abi.nv_of(cfg)
     out = []
     for v in range(nv):
         a, b, z = interior(cfg, U[..., v]), interior(cfg, Uref[..., v]), interior(cfg, U0[..., v])
-        st = rel_l2(a, b)
+        st = rel_l2(a, b) if np.abs(z).max() > 0 else 0.0
         inc = rel_l2(a - z, b - z) if np.abs(b - z).max() > 0 else 0.0
         out.append((v, st, inc))
     return out
