@@ -317,7 +317,7 @@ __device__ __forceinline__ bool smooth_at(const unsigned char* map, long long c,
 // when computing a bare right-hand side.
 // ---------------------------------------------------------------------------
 template <int NV, bool HYB>
-__global__ void __launch_bounds__(TX * TY) k_mrhs3d(Geo g, Phys P, MixedView M,
+__global__ void __launch_bounds__(TX * TY, 3) k_mrhs3d(Geo g, Phys P, MixedView M,
                                                     const unsigned long long* __restrict__ red,
                                                     const unsigned char* __restrict__ smap,
                                                     const double* Uold, double* Unew, double coef,
