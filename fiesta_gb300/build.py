@@ -30,6 +30,7 @@ UNITS = [
     ("fst_mixed.cu", ["--use_fast_math"]),
     ("fst_hybrid.cu", ["--use_fast_math"]),
     ("fst_api.cu", ["--fmad=false"]),
+    ("fst_noalloc.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["fst_host.cpp"]
 

@@ -247,6 +247,29 @@ int bcs(fst_ctx* c, double* U) {
 
 }  // namespace
 
+// Geometry and physics constants of a config, for entry points that run
+// without a context (fst_noalloc.cu).  Returns "" or the validation error.
+std::string fst_setup_geo_phys(const fst_config* cfg, Geo& g, Phys& P) {
+  std::string why = validate(cfg);
+  if (!why.empty()) return why;
+  g.ndim = cfg->ndim;
+  g.ng = cfg->ng;
+  g.nci = cfg->nci;
+  g.ncj = cfg->ncj;
+  g.nck = g.ndim == 3 ? cfg->nck : 1;
+  g.ngi = g.nci + 2 * g.ng;
+  g.ngj = g.ncj + 2 * g.ng;
+  g.ngk = g.ndim == 3 ? g.nck + 2 * g.ng : 1;
+  g.ns = cfg->ns;
+  g.nv = (g.ndim == 3 ? 4 : 3) + g.ns;
+  g.nvt = g.nv + (cfg->ceq ? 5 : 0);
+  g.sy = g.ngi;
+  g.sz = (long long)g.ngi * g.ngj;
+  g.sv = g.sz * g.ngk;
+  setup_phys(*cfg, g, P);
+  return "";
+}
+
 extern "C" {
 
 const char* fst_last_error(const fst_ctx* c) { return c ? c->err.c_str() : "null context"; }

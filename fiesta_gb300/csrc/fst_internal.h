@@ -56,6 +56,9 @@ struct Prof {
     ++(n);                                  \
   } while (0)
 
+// fst_api.cu
+std::string fst_setup_geo_phys(const fst_config* cfg, Geo& g, Phys& P);
+
 // fst_bc.cu
 int fst_launch_bcs(const Geo& g, const fst_config& cf, double* U, cudaStream_t stream, Prof* prof);
 

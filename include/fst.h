@@ -187,6 +187,29 @@ typedef struct fst_kernel_time {
 int fst_set_profiling(fst_ctx* ctx, int on);
 int fst_kernel_times(fst_ctx* ctx, fst_kernel_time* out, int max, int* count);
 
+/* Allocation-free 2D right-hand side.  No counterpart in the reference: it
+ * serves host programs that own every byte of device memory themselves (a
+ * fixed pre-reserved pool, a Fortran or legacy host that forbids allocation
+ * after start-up, a loop that cannot afford the implicit device-wide
+ * synchronisation of cudaMalloc/cudaFree) and so cannot create an fst_ctx.
+ *
+ * Computes the plain FP64 right-hand side of cart2d_func::compute for the
+ * device state d_U (LayoutLeft, ghosts already filled, n = fst_state_size())
+ * into device memory d_R (same layout; zero outside the interior), on
+ * `cuda_stream` (NULL: the default stream).  cfg must be 2D plain FP64.
+ * Work arrays live in one fixed device array of FST_NOALLOC_SCRATCH_BYTES
+ * inside the library (held by every GPU that loads it until exit); grids of
+ * more than FST_NOALLOC_MAX_CELLS cells including ghosts (ngi*ngj) are
+ * rejected with FST_ERR_SIZE.  Nothing is allocated or freed.
+ * The first call on each device looks up that device's copy of the array
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (different
+ * streams or host threads without ordering between them) race. */
+#define FST_NOALLOC_MAX_CELLS 16384
+#define FST_NOALLOC_SCRATCH_BYTES (8u << 20)
+int fst_rhs2d_noalloc(const fst_config* cfg, const double* d_U, double* d_R, size_t n,
+                      void* cuda_stream);
+
 /* Seeded initial conditions generated on the host (same on every platform;
  * no libm calls).  `kind`: FST_IC_*.  Writes the interior of U (LayoutLeft,
  * n = fst_state_size()); ghosts and C variables are set to zero. */
