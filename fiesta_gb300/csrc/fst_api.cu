@@ -172,6 +172,7 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
   P.mu2d_f = (float)P.mu2d;
   P.kheat_f = (float)P.kheat2d;
   for (int s = 0; s < g.ns; ++s) {
+    P.rm_s[s] = P.cp_s[s] - P.cv_s[s];
     P.cv_f[s] = (float)P.cv_s[s];
     P.rm_f[s] = (float)(P.cp_s[s] - P.cv_s[s]);
     P.mu_f[s] = (float)P.mu_s[s];

@@ -35,6 +35,7 @@ struct Phys {
   // species constants of calculateRhoPT (src/secondary.hpp:127-135):
   //   cp_s = gammas*Rs/(gammas-1), cv_s = Rs/(gammas-1), Rs = cd(7+3s)
   double cp_s[FST_MAX_SPECIES], cv_s[FST_MAX_SPECIES], mu_s[FST_MAX_SPECIES];
+  double rm_s[FST_MAX_SPECIES];  // cp_s - cv_s = Rs (mixed path)
   // the same with the stride-2 species table read by maxWaveSpeed2D
   // (src/ceq.hpp:61-66): gammas = cd(6+2s), Rs = cd(7+2s)
   double cp2_s[FST_MAX_SPECIES], cv2_s[FST_MAX_SPECIES];

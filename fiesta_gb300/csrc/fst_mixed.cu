@@ -69,15 +69,13 @@ __device__ __forceinline__ double f2d(float x) {
   return __hiloint2double((int)hi, e == 0u ? 0 : (int)(m << 29));
 }
 
-// FP64 reciprocal by two Newton-Raphson steps from an FP32 seed (relative
-// error ~1e-16 for arguments inside the FP32 range, which holds for the
-// densities and heat capacities it is used on).
+// FP64 reciprocal by one Newton-Raphson step from the correctly rounded FP32
+// reciprocal: relative error below ~1e-14 (the square of the seed's 2^-24),
+// for arguments inside the FP32 range, which holds for the densities and heat
+// capacities it is used on.
 __device__ __forceinline__ double rcp64(double x) {
-  double r = f2d(__frcp_rn(d2f(x)));
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
+  const double r = f2d(__frcp_rn(d2f(x)));
+  return fma(r, fma(-x, r, 1.0), r);
 }
 
 __device__ __forceinline__ float warp_maxf(float v) {
@@ -109,7 +107,7 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __re
       const double rs = U[c + sv * (s0 + s)];
       r += rs;
       sCv = fma(rs, P.cv_s[s], sCv);
-      sRm = fma(rs, P.cp_s[s] - P.cv_s[s], sRm);
+      sRm = fma(rs, P.rm_s[s], sRm);
     }
     const double ri = rcp64(r);
     const double gm1 = sRm * rcp64(sCv);
