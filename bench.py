@@ -238,6 +238,62 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
     }
 
 
+def run_batch2d(steps, warmup, ncases=64):
+    """The batched 2D ensemble (64 RT cases, n log-uniform in [128, 1024]):
+    aggregate Mcell-steps/s with one persistent launch per stage under CUDA
+    graph replay, against the same cases stepped one context at a time."""
+    import torch
+    from fiesta_gb300.batch import Batch, rt_ensemble
+    from fiesta_gb300.solver import Solver
+    cfgs, states = rt_ensemble(ncases=ncases)
+    cells = sum(c.nci * c.ncj for c in cfgs)
+    b = Batch(cfgs)
+    for c, U in enumerate(states):
+        b.set_state(c, U)
+    tune_path = os.path.join(ROOT, "fiesta_gb300", "tune_batch2d.json")
+    h = b.tune(tune_path)
+    b.rk_step(warmup)
+    b.synchronize()
+    st = torch.cuda.ExternalStream(b.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.rk_step(steps)
+    e1.record(st)
+    b.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    info = b.info()
+    b.close()
+    # one context (one set of launches) per case
+    ctxs = []
+    for cfg, U in zip(cfgs, states):
+        s = Solver(cfg)
+        s.set_state(U)
+        ctxs.append(s)
+    stream = torch.cuda.current_stream()
+    for s in ctxs:
+        s.set_stream(stream.cuda_stream)
+    for _ in range(warmup):
+        for s in ctxs:
+            s.rk_step(1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        for s in ctxs:
+            s.rk_step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms1 = e0.elapsed_time(e1) / steps
+    for s in ctxs:
+        s.close()
+    return {"value": cells / (ms / 1e3) / 1e6, "unit": "Mcell-steps/s", "ms_per_step": ms,
+            "one_launch_per_case": cells / (ms1 / 1e3) / 1e6, "ms_per_step_per_case_launches": ms1,
+            "ncases": ncases, "interior_cells": cells, "tile_height": h,
+            "persistent_blocks": info["persistent_blocks"],
+            "launches_per_step": info["launches_per_step"],
+            "workload": "64 2D RT cases, n log-uniform in [128,1024], 2 species, viscous, "
+                        "C-equation, buoyancy; mixed precision; CUDA graph per step"}
+
+
 def cpu_sample(n_sample=128, steps=1):
     """The CPU oracle (restatement of the reference's FP64 path) on a bounded
     sample of the same workload, all host threads."""
@@ -271,6 +327,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -329,6 +386,7 @@ def main():
         value = world * (n ** 3) / (ms / 1e3) / 1e6
     if rank != 0:
         return
+    batch = None if a.no_batch else run_batch2d(a.steps, a.warmup)
     cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
@@ -342,6 +400,7 @@ def main():
         "roofline": r["roofline"], "cpu_baseline": cpu, "clocks": r["clocks"],
         "e2e": r["e2e"], "gpu_launches": r["gpu_launches"],
         "modes": {m: {k: v for k, v in results[m].items() if k not in ("clocks",)} for m in modes},
+        "batch2d": batch,
     }
     print(json.dumps(line))
 

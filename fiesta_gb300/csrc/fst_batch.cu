@@ -1,0 +1,568 @@
+// fst_batch.cu — many independent 2D cases of uneven size stepped together
+// (the batched RT / rising-bubble ensemble), mixed precision.
+//
+// Per RK stage the ensemble is advanced by a fixed set of launches that
+// cover every case at once, instead of one set per case:
+//   k_bface / k_bperiodic  ghost fills, one launch per fill step, grid.y = case
+//   k_binit                reset the per-case C-equation maxima
+//   k_bprim                primitive pass over the concatenated cells of all
+//                          cases (block ranges aligned to cases, so a block's
+//                          per-case maxima reduce to one atomicMax per warp)
+//   k_brhs                 one persistent launch per stage: #SM x occupancy
+//                          blocks walk a global list of (case, tile) work items
+//                          and run the fused 2D RHS + RK tile of fst_mixed
+//   k_bghost               stage-1 ghost copy
+// A whole time step is captured once into a CUDA graph and replayed.  The
+// tile height (threads along j) is picked by an autotuner that times the
+// candidates on the actual ensemble and persists the choice to a JSON file
+// keyed by GPU and ensemble signature.
+//
+// The per-cell and per-tile arithmetic is the single-case mixed path's
+// (fst_mixed_dev.cuh), so a batched case evolves exactly like the same case
+// run alone in FST_MODE_MIXED (tests/test_gpu_batch.py).
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "fst_bc_dev.cuh"
+#include "fst_mixed_dev.cuh"
+
+using namespace fstm;
+
+namespace {
+
+struct BCase {
+  Geo g;
+  MixedView M;
+  double *Ua, *Ub;
+  unsigned long long* red;  // 2 keys
+  float* Q;                 // writable views of the mixed buffers
+  float *rho32, *vel32, *T32, *nrg, *C;
+  double *p64, *rho64;
+  int bc[4];     // xmin, xmax, ymin, ymax
+  int per[2];    // x, y periodic
+};
+
+constexpr int kTileHeights[3] = {4, 8, 16};
+
+__device__ __forceinline__ int find_case(const int* __restrict__ off, int n, int x) {
+  // largest c with off[c] <= x (off has n+1 entries, off[0] = 0)
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_binit(const BCase* __restrict__ cs, int n) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) {
+    cs[c].red[0] = FST_KEY_LOWEST;
+    cs[c].red[1] = FST_KEY_LOWEST;
+  }
+}
+
+// ghost fills: grid.y = case, grid.x over the case's ghost lines
+__global__ void k_bperiodic(const BCase* __restrict__ cs, int axis, bool use_a) {
+  const BCase& B = cs[blockIdx.y];
+  if (!B.per[axis]) return;
+  const Geo& g = B.g;
+  const int na = axis == 0 ? g.ngj : g.ngi;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * g.nvt) return;
+  fstbc::periodic_line(g, use_a ? B.Ua : B.Ub, axis, (int)(t % na), 0, (int)(t / na));
+}
+
+__global__ void k_bface(const BCase* __restrict__ cs, int axis, int side, bool use_a) {
+  const BCase& B = cs[blockIdx.y];
+  if (B.per[axis]) return;
+  const Geo& g = B.g;
+  const int na = axis == 0 ? g.ngj : g.ngi;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= na) return;
+  fstbc::face_line(g, use_a ? B.Ua : B.Ub, axis, side, B.bc[axis * 2 + side], t, 0);
+}
+
+// primitive pass: block b belongs to case find_case(block_off, b)
+__global__ void __launch_bounds__(256) k_bprim(const BCase* __restrict__ cs,
+                                               const Phys* __restrict__ Ps,
+                                               const int* __restrict__ block_off, int ncase,
+                                               bool use_a, bool red) {
+  const int c = find_case(block_off, ncase, blockIdx.x);
+  const BCase& B = cs[c];
+  const Geo& g = B.g;
+  const int local = (blockIdx.x - block_off[c]) * blockDim.x + threadIdx.x;
+  float lS = -3.0e38f, lC = -3.0e38f;
+  if (local < (int)g.sv) {
+    const int i = local % g.ngi, j = local / g.ngi;
+    mprim_cell<2>(g, Ps[c], use_a ? B.Ua : B.Ub, B.Q, B.rho32, B.rho64, B.vel32, B.p64, nullptr,
+                  B.nrg, B.C, B.T32, red, i, j, 0, lS, lC);
+  }
+  if (red) {
+    lS = warp_maxf(lS);
+    lC = warp_maxf(lC);
+    if ((threadIdx.x & 31) == 0 && lS > -1e38f) {
+      atomicMax(&B.red[0], fst_key((double)lS));
+      atomicMax(&B.red[1], fst_key((double)lC));
+    }
+  }
+}
+
+// stage-1 ghost copy U1 = U + (0.5*dt)*0 on ghost cells (src/rk.cpp:42-50)
+__global__ void k_bghost(const BCase* __restrict__ cs, const int* __restrict__ block_off,
+                         int ncase) {
+  const int c = find_case(block_off, ncase, blockIdx.x);
+  const BCase& B = cs[c];
+  const Geo& g = B.g;
+  const int local = (blockIdx.x - block_off[c]) * blockDim.x + threadIdx.x;
+  if (local >= (int)g.sv) return;
+  const int i = local % g.ngi, j = local / g.ngi;
+  if (i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng) return;
+  for (int v = 0; v < g.nvt; ++v) B.Ub[local + g.sv * v] = B.Ua[local + g.sv * v];
+}
+
+// persistent RHS + RK stage over the (case, tile) work list
+template <int NV, int TYY>
+__global__ void __launch_bounds__(TX * TYY) k_brhs(const BCase* __restrict__ cs,
+                                                   const Phys* __restrict__ Ps,
+                                                   const int* __restrict__ tile_off, int ncase,
+                                                   int stage) {
+  __shared__ float sG[TYY][TX][NV];
+  const int ntile = tile_off[ncase];
+  for (int w = blockIdx.x; w < ntile; w += gridDim.x) {
+    const int c = find_case(tile_off, ncase, w);
+    const BCase& B = cs[c];
+    const Phys& P = Ps[c];
+    const int ntx = (B.g.nci + TX - 2) / (TX - 1);
+    const int local = w - tile_off[c];
+    const double* Uin = stage == 1 ? B.Ua : B.Ub;
+    (void)Uin;
+    // stage 1: Ub = Ua + hdt*R(Ua); stage 2: Ua = Ua + dt*R(Ub)
+    rhs2d_tile<NV, false, TYY>(B.g, P, B.M, B.red, nullptr, B.Ua, stage == 1 ? B.Ub : B.Ua,
+                               stage == 1 ? P.hdt : P.dt, nullptr, local % ntx, local / ntx, sG);
+    __syncthreads();
+  }
+}
+
+inline unsigned cdivu(long long a, int b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace
+
+struct fst_batch {
+  std::vector<fst_config> cfgs;
+  std::vector<Geo> geos;
+  std::vector<Phys> phys;
+  std::vector<BCase> hcases;
+  BCase* dcases = nullptr;
+  Phys* dphys = nullptr;
+  int* dblock_off = nullptr;
+  int* dtile_off = nullptr;
+  int nblocks = 0;
+  int ntiles = 0;
+  int nv = 0, nvt = 0;
+  int tile_h = 8;
+  int max_lines = 0, max_face = 0;
+  int persistent_blocks = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void*> allocs;
+  std::string err;
+  long long launches = 0;
+};
+
+namespace {
+
+int bfail(fst_batch* b, int code, const std::string& m) {
+  b->err = m;
+  return code;
+}
+
+int balloc(fst_batch* b, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, FST_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  b->allocs.push_back(*p);
+  cudaMemsetAsync(*p, 0, bytes, b->stream);
+  return FST_OK;
+}
+
+// launches of one RK stage; returns launch count
+template <int NV, int TYY>
+int enqueue_rhs(fst_batch* b, int stage) {
+  k_brhs<NV, TYY><<<b->persistent_blocks, dim3(TX, TYY, 1), 0, b->stream>>>(
+      b->dcases, b->dphys, b->dtile_off, (int)b->hcases.size(), stage);
+  return 1;
+}
+
+template <int TYY>
+int enqueue_rhs_nv(fst_batch* b, int stage) {
+  switch (b->nv) {
+    case 4: return enqueue_rhs<4, TYY>(b, stage);
+    case 5: return enqueue_rhs<5, TYY>(b, stage);
+    case 6: return enqueue_rhs<6, TYY>(b, stage);
+    case 7: return enqueue_rhs<7, TYY>(b, stage);
+    case 8: return enqueue_rhs<8, TYY>(b, stage);
+    default: return enqueue_rhs<NVMAX, TYY>(b, stage);
+  }
+}
+
+template <int TYY>
+const void* rhs_kernel(int nv) {
+  switch (nv) {
+    case 4: return (const void*)k_brhs<4, TYY>;
+    case 5: return (const void*)k_brhs<5, TYY>;
+    case 6: return (const void*)k_brhs<6, TYY>;
+    case 7: return (const void*)k_brhs<7, TYY>;
+    case 8: return (const void*)k_brhs<8, TYY>;
+    default: return (const void*)k_brhs<NVMAX, TYY>;
+  }
+}
+
+// tile list for the chosen tile height; persistent grid size by occupancy
+int setup_tiles(fst_batch* b) {
+  const int n = (int)b->hcases.size();
+  std::vector<int> off(n + 1, 0);
+  for (int c = 0; c < n; ++c) {
+    const Geo& g = b->geos[c];
+    const int ntx = (g.nci + TX - 2) / (TX - 1);
+    const int nty = (g.ncj + b->tile_h - 2) / (b->tile_h - 1);
+    off[c + 1] = off[c] + ntx * nty;
+  }
+  b->ntiles = off[n];
+  cudaError_t e = cudaMemcpyAsync(b->dtile_off, off.data(), sizeof(int) * (n + 1),
+                                  cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
+  const void* k = b->tile_h == 4 ? rhs_kernel<4>(b->nv)
+                  : b->tile_h == 8 ? rhs_kernel<8>(b->nv) : rhs_kernel<16>(b->nv);
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TX * b->tile_h, 0);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  b->persistent_blocks = std::max(1, per_sm) * sms;
+  return FST_OK;
+}
+
+int enqueue_step(fst_batch* b) {
+  const int n = (int)b->hcases.size();
+  int L = 0;
+  auto bcs = [&](bool use_a) {
+    for (int ax = 0; ax < 2; ++ax) {
+      k_bperiodic<<<dim3(cdivu((long long)b->max_lines * b->nvt, 128), n), 128, 0, b->stream>>>(
+          b->dcases, ax, use_a);
+      ++L;
+    }
+    for (int ax = 0; ax < 2; ++ax)
+      for (int side = 0; side < 2; ++side) {
+        k_bface<<<dim3(cdivu(b->max_face, 128), n), 128, 0, b->stream>>>(b->dcases, ax, side,
+                                                                           use_a);
+        ++L;
+      }
+  };
+  const bool ceq = b->cfgs[0].ceq != 0;
+  bcs(true);  // cart2d_func::preStep
+  for (int stage = 1; stage <= 2; ++stage) {
+    const bool use_a = stage == 1;
+    if (ceq) {
+      k_binit<<<cdivu(n, 64), 64, 0, b->stream>>>(b->dcases, n);
+      ++L;
+    }
+    k_bprim<<<b->nblocks, 256, 0, b->stream>>>(b->dcases, b->dphys, b->dblock_off, n, use_a, ceq);
+    ++L;
+    if (b->tile_h == 4) L += enqueue_rhs_nv<4>(b, stage);
+    else if (b->tile_h == 8) L += enqueue_rhs_nv<8>(b, stage);
+    else L += enqueue_rhs_nv<16>(b, stage);
+    if (stage == 1) {
+      k_bghost<<<b->nblocks, 256, 0, b->stream>>>(b->dcases, b->dblock_off, n);
+      ++L;
+    }
+  }
+  return L;
+}
+
+int capture(fst_batch* b) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  const int L = enqueue_step(b);
+  e = cudaStreamEndCapture(b->stream, &b->graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e));
+  b->launches = L;
+  return FST_OK;
+}
+
+std::string signature(const fst_batch* b) {
+  cudaDeviceProp prop;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaGetDeviceProperties(&prop, dev);
+  long long cells = 0;
+  for (auto& g : b->geos) cells += (long long)g.nci * g.ncj;
+  std::ostringstream s;
+  s << prop.name << "|cases=" << b->geos.size() << "|cells=" << cells << "|nv=" << b->nv
+    << "|visc=" << b->cfgs[0].visc << "|ceq=" << b->cfgs[0].ceq;
+  return s.str();
+}
+
+}  // namespace
+
+extern "C" {
+
+int fst_batch_create(const fst_config* cfgs, int ncases, fst_batch** out) {
+  if (!cfgs || ncases < 1 || !out) return FST_ERR_INVALID;
+  *out = nullptr;
+  fst_batch* b = new fst_batch();
+  for (int c = 0; c < ncases; ++c) {
+    const fst_config& cf = cfgs[c];
+    Geo g;
+    Phys P;
+    std::string why = fst_setup_geo_phys(&cf, g, P);
+    if (why.empty() && cf.ndim != 2) why = "batched cases must be 2D";
+    if (why.empty() && cf.mode != FST_MODE_MIXED) why = "batched cases run in FST_MODE_MIXED";
+    if (why.empty() && c > 0 &&
+        (cf.ns != cfgs[0].ns || cf.visc != cfgs[0].visc || cf.ceq != cfgs[0].ceq ||
+         cf.buoyancy != cfgs[0].buoyancy))
+      why = "batched cases must share ns and the visc/ceq/buoyancy switches";
+    if (!why.empty()) {
+      std::fprintf(stderr, "fst_batch_create: case %d: %s\n", c, why.c_str());
+      delete b;
+      return FST_ERR_INVALID;
+    }
+    b->cfgs.push_back(cf);
+    b->geos.push_back(g);
+    b->phys.push_back(P);
+  }
+  b->nv = b->geos[0].nv;
+  b->nvt = b->geos[0].nvt;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return FST_ERR_CUDA;
+  }
+  b->own_stream = true;
+  int rc = FST_OK;
+  std::vector<int> boff(ncases + 1, 0);
+  for (int c = 0; c < ncases && !rc; ++c) {
+    const Geo& g = b->geos[c];
+    const fst_config& cf = b->cfgs[c];
+    const size_t n = (size_t)g.sv;
+    BCase B{};
+    B.g = g;
+    auto A = [&](void** p, size_t bytes) {
+      if (!rc) rc = balloc(b, p, bytes);
+    };
+    A((void**)&B.Ua, sizeof(double) * n * g.nvt);
+    A((void**)&B.Ub, sizeof(double) * n * g.nvt);
+    A((void**)&B.red, sizeof(unsigned long long) * 2);
+    A((void**)&B.Q, sizeof(float) * n * g.nv);
+    A((void**)&B.rho32, sizeof(float) * n);
+    A((void**)&B.vel32, sizeof(float) * n * 2);
+    A((void**)&B.p64, sizeof(double) * n);
+    if (cf.buoyancy) A((void**)&B.rho64, sizeof(double) * n);
+    if (cf.visc) A((void**)&B.T32, sizeof(float) * n);
+    if (cf.ceq) {
+      A((void**)&B.nrg, sizeof(float) * n);
+      A((void**)&B.C, sizeof(float) * n * 5);
+    }
+    B.M = MixedView{B.Q, B.rho32, B.vel32, B.p64, nullptr, B.nrg, B.C, B.T32, B.rho64};
+    B.bc[0] = cf.bc_xmin;
+    B.bc[1] = cf.bc_xmax;
+    B.bc[2] = cf.bc_ymin;
+    B.bc[3] = cf.bc_ymax;
+    B.per[0] = cf.xper != 0;
+    B.per[1] = cf.yper != 0;
+    b->hcases.push_back(B);
+    boff[c + 1] = boff[c] + (int)((n + 255) / 256);
+    b->max_lines = std::max(b->max_lines, std::max(g.ngi, g.ngj));
+    b->max_face = std::max(b->max_face, std::max(g.ngi, g.ngj));
+  }
+  b->nblocks = boff[ncases];
+  if (!rc) rc = balloc(b, (void**)&b->dcases, sizeof(BCase) * ncases);
+  if (!rc) rc = balloc(b, (void**)&b->dphys, sizeof(Phys) * ncases);
+  if (!rc) rc = balloc(b, (void**)&b->dblock_off, sizeof(int) * (ncases + 1));
+  if (!rc) rc = balloc(b, (void**)&b->dtile_off, sizeof(int) * (ncases + 1));
+  if (!rc) {
+    e = cudaMemcpyAsync(b->dcases, b->hcases.data(), sizeof(BCase) * ncases,
+                        cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->dphys, b->phys.data(), sizeof(Phys) * ncases, cudaMemcpyHostToDevice,
+                          b->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->dblock_off, boff.data(), sizeof(int) * (ncases + 1),
+                          cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (!rc) rc = setup_tiles(b);
+  if (!rc) rc = capture(b);
+  if (rc) {
+    std::fprintf(stderr, "fst_batch_create: %s\n", b->err.c_str());
+    fst_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return FST_OK;
+}
+
+void fst_batch_destroy(fst_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+const char* fst_batch_last_error(const fst_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int fst_batch_set_state(fst_batch* b, int c, const double* U, size_t n) {
+  if (!b || !U || c < 0 || c >= (int)b->hcases.size()) return FST_ERR_INVALID;
+  const Geo& g = b->geos[c];
+  if (n != (size_t)g.sv * g.nvt) return bfail(b, FST_ERR_SIZE, "state size mismatch");
+  cudaError_t e = cudaMemcpyAsync(b->hcases[c].Ua, U, n * sizeof(double), cudaMemcpyHostToDevice,
+                                  b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FST_OK : bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int fst_batch_get_state(fst_batch* b, int c, double* U, size_t n) {
+  if (!b || !U || c < 0 || c >= (int)b->hcases.size()) return FST_ERR_INVALID;
+  const Geo& g = b->geos[c];
+  if (n != (size_t)g.sv * g.nvt) return bfail(b, FST_ERR_SIZE, "state size mismatch");
+  cudaError_t e = cudaMemcpyAsync(U, b->hcases[c].Ua, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                  b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FST_OK : bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int fst_batch_rk_step(fst_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return FST_ERR_INVALID;
+  for (int s = 0; s < nsteps; ++s) {
+    cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+    if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  }
+  return FST_OK;
+}
+
+int fst_batch_synchronize(fst_batch* b) {
+  if (!b) return FST_ERR_INVALID;
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FST_OK : bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
+}
+
+void* fst_batch_stream(fst_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int fst_batch_set_tile_height(fst_batch* b, int h) {
+  if (!b || (h != 4 && h != 8 && h != 16)) return FST_ERR_INVALID;
+  b->tile_h = h;
+  int rc = setup_tiles(b);
+  return rc ? rc : capture(b);
+}
+
+int fst_batch_info(const fst_batch* b, fst_batch_info_t* out) {
+  if (!b || !out) return FST_ERR_INVALID;
+  out->ncases = (int)b->hcases.size();
+  out->tile_height = b->tile_h;
+  out->tiles = b->ntiles;
+  out->persistent_blocks = b->persistent_blocks;
+  out->launches_per_step = (int)b->launches;
+  long long cells = 0;
+  for (auto& g : b->geos) cells += (long long)g.nci * g.ncj;
+  out->interior_cells = cells;
+  return FST_OK;
+}
+
+int fst_batch_tune(fst_batch* b, const char* json_path, int force) {
+  if (!b) return FST_ERR_INVALID;
+  const std::string key = signature(b);
+  std::string text;
+  if (json_path) {
+    std::ifstream f(json_path);
+    if (f) {
+      std::stringstream ss;
+      ss << f.rdbuf();
+      text = ss.str();
+    }
+  }
+  const std::string needle = "\"key\": \"" + key + "\", \"tile_height\": ";
+  const size_t at = text.find(needle);
+  if (!force && at != std::string::npos) {
+    const int h = std::atoi(text.c_str() + at + needle.size());
+    return fst_batch_set_tile_height(b, h);
+  }
+  // time each candidate on a few steps of this ensemble (state is restored)
+  std::vector<std::vector<double>> saved(b->hcases.size());
+  for (size_t c = 0; c < b->hcases.size(); ++c) {
+    saved[c].resize((size_t)b->geos[c].sv * b->geos[c].nvt);
+    int rc = fst_batch_get_state(b, (int)c, saved[c].data(), saved[c].size());
+    if (rc) return rc;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e300;
+  int best_h = 8;
+  std::ostringstream times;
+  for (int h : kTileHeights) {
+    int rc = fst_batch_set_tile_height(b, h);
+    if (rc) return rc;
+    fst_batch_rk_step(b, 1);
+    cudaEventRecord(e0, b->stream);
+    fst_batch_rk_step(b, 3);
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    times << (times.tellp() > 0 ? ", " : "") << "\"" << h << "\": " << ms / 3.0;
+    if (ms < best) {
+      best = ms;
+      best_h = h;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (size_t c = 0; c < b->hcases.size(); ++c)
+    fst_batch_set_state(b, (int)c, saved[c].data(), saved[c].size());
+  int rc = fst_batch_set_tile_height(b, best_h);
+  if (rc) return rc;
+  if (json_path) {
+    // one entry per line inside {"entries": [ ... ]}
+    std::vector<std::string> lines;
+    std::istringstream in(text);
+    std::string ln;
+    while (std::getline(in, ln))
+      if (ln.find("\"key\": ") != std::string::npos && ln.find(needle) == std::string::npos) {
+        while (!ln.empty() && (ln.back() == ',' || ln.back() == ' ')) ln.pop_back();
+        lines.push_back(ln);
+      }
+    std::ostringstream entry;
+    entry << "  {" << needle << best_h << ", \"ms_per_step\": {" << times.str() << "}}";
+    lines.push_back(entry.str());
+    std::ofstream f(json_path);
+    f << "{\"entries\": [\n";
+    for (size_t q = 0; q < lines.size(); ++q) f << lines[q] << (q + 1 < lines.size() ? ",\n" : "\n");
+    f << "]}\n";
+  }
+  return FST_OK;
+}
+
+}  // extern "C"

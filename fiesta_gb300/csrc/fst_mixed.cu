@@ -31,58 +31,10 @@
 // (src/flux.hpp, src/viscosity.hpp, src/ceq3d.hpp, src/ceq.hpp,
 // src/presgrad.hpp, src/buoyancy.hpp); only the arithmetic precision differs.
 // The error against the FP64 oracle is measured by tests/test_gpu_mixed.py.
-#include "fst_internal.h"
+#include "fst_mixed_dev.cuh"
 
 namespace {
-
-constexpr int TX = 32;  // tile width (threads along i)
-constexpr int TY = 8;   // tile height (threads along j)
-constexpr int KZ = 16;  // planes per block along k
-constexpr int NVMAX = 4 + FST_MAX_SPECIES;
-
-// ---------------------------------------------------------------------------
-// primitives
-// ---------------------------------------------------------------------------
-// FP64 <-> FP32 conversions on the integer pipe.  GB300's FP64 unit also
-// executes the F2F conversions, at the FP64 rate; these rebias the exponent
-// and round the mantissa with integer operations instead.  Values outside
-// the FP32 normal range go to signed zero / infinity (no FP32 denormals);
-// NaN stays NaN; mantissa ties round away from zero.
-__device__ __forceinline__ float d2f(double x) {
-  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
-  const unsigned int sign = hi & 0x80000000u;
-  const unsigned int ex = (hi >> 20) & 0x7FFu;
-  const int e = (int)ex - 1023 + 127;
-  const unsigned int m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-  const unsigned int r = (lo >> 28) & 1u;
-  unsigned int bits = (((unsigned int)e << 23) | m) + r;  // a carry rounds into the exponent
-  if (e <= 0) bits = 0u;
-  if (e >= 255) bits = (ex == 0x7FFu && ((hi & 0xFFFFFu) | lo)) ? 0x7FC00000u : 0x7F800000u;
-  return __uint_as_float(sign | bits);
-}
-__device__ __forceinline__ double f2d(float x) {
-  const unsigned int f = __float_as_uint(x);
-  const unsigned int sign = f & 0x80000000u, e = (f >> 23) & 0xFFu, m = f & 0x7FFFFFu;
-  unsigned int hi = sign | ((e + 896u) << 20) | (m >> 3);
-  if (e == 0u) hi = sign;                                   // zero (and FP32 denormals)
-  if (e == 255u) hi = sign | 0x7FF00000u | (m >> 3) | (m ? 0x80000u : 0u);  // inf / NaN
-  return __hiloint2double((int)hi, e == 0u ? 0 : (int)(m << 29));
-}
-
-// FP64 reciprocal by one Newton-Raphson step from the correctly rounded FP32
-// reciprocal: relative error below ~1e-14 (the square of the seed's 2^-24),
-// for arguments inside the FP32 range, which holds for the densities and heat
-// capacities it is used on.
-__device__ __forceinline__ double rcp64(double x) {
-  const double r = f2d(__frcp_rn(d2f(x)));
-  return fma(r, fma(-x, r, 1.0), r);
-}
-
-__device__ __forceinline__ float warp_maxf(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
+using namespace fstm;
 
 template <int NDIM>
 __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __restrict__ U,
@@ -94,71 +46,10 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __re
                                                unsigned long long* __restrict__ red) {
   // grid: x covers i in blocks of 256, y = j, z = k (no integer division)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, k = blockIdx.z;
-  const long long sv = g.sv;
   float lS = -3.0e38f, lC = -3.0e38f;
-  if (i < g.ngi) {
-    const long long c = (long long)i + g.sy * j + g.sz * k;
-    const int s0 = NDIM + 1;  // first species index
-    // mixture EOS in FP64 (calculateRhoPT, src/secondary.hpp:60-151):
-    // gamma - 1 = R_mix / Cv = (sum rho_s R_s) / (sum rho_s cv_s)
-    double r = 0.0, sCv = 0.0, sRm = 0.0;
-    for (int s = 0; s < P.ns; ++s) {
-      const double rs = U[c + sv * (s0 + s)];
-      r += rs;
-      sCv = fma(rs, P.cv_s[s], sCv);
-      sRm = fma(rs, P.rm_s[s], sRm);
-    }
-    const double ri = rcp64(r);
-    const double gm1 = sRm * rcp64(sCv);
-    const float rif = d2f(ri);
-    float Cv2 = 0.f, Cp2 = 0.f;
-    for (int s = 0; s < P.ns; ++s) {
-      const float rs = d2f(U[c + sv * (s0 + s)]);
-      const float ys = rs * rif;
-      if (NDIM == 2) {
-        Cv2 += ys * P.cv2_f[s];
-        Cp2 += ys * P.cp2_f[s];
-      }
-      if (Y) Y[c + sv * s] = ys;
-      Q[c + sv * (s0 + s)] = rs;
-    }
-    double msq = 0.0;
-    float usq = 0.f;
-#pragma unroll
-    for (int d = 0; d < NDIM; ++d) {
-      const double m = U[c + sv * d];
-      msq = fma(m, m, msq);
-      const float mf = d2f(m);
-      const float u = mf * rif;
-      usq += u * u;
-      vel[c + sv * d] = u;
-      Q[c + sv * d] = mf;
-    }
-    const double E = U[c + sv * NDIM];
-    const double p = gm1 * (E - 0.5 * msq * ri);  // FP64 pressure recovery
-    pr[c] = p;
-    Q[c + sv * NDIM] = d2f(E + p);
-    const float rf = d2f(r);
-    rho[c] = rf;
-    if (rho64) rho64[c] = r;
-    if (T) T[c] = d2f(p) * rif / d2f(sRm * ri);
-    if (nrg) nrg[c] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
-    if (Cc)
-      for (int n = 0; n < 5; ++n) Cc[c + sv * n] = d2f(U[c + sv * (P.nv + n)]);
-    if (red) {
-      const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
-                      (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
-      if (in) {
-        const float pf = d2f(p), mf = sqrtf(d2f(msq));
-        float s;
-        if (NDIM == 3) s = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
-        else s = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
-        lS = fmaxf(lS, s);
-        lC = fmaxf(lC, fabsf(Cc[c + sv]));
-      }
-    }
-  }
+  if (i < g.ngi)
+    mprim_cell<NDIM>(g, P, U, Q, rho, rho64, vel, pr, Y, nrg, Cc, T, red != nullptr, i,
+                     blockIdx.y, blockIdx.z, lS, lC);
   if (red) {
     lS = warp_maxf(lS);
     lC = warp_maxf(lC);
@@ -167,147 +58,6 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __re
       atomicMax(&red[1], fst_key((double)lC));
     }
   }
-}
-
-// ---------------------------------------------------------------------------
-// FP32 WENO5-JS with the reference's weights (src/flux.hpp:241-266); the
-// nonlinear weights are scaled by the smallest (eps+beta) so that no square
-// overflows or underflows in FP32 (the normalised weights are unchanged).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float weno_f(float f1, float f2, float f3, float f4, float f5) {
-  const float eps = 1e-6f;
-  float a1 = f1 - 2.0f * f2 + f3, a2 = f1 - 4.0f * f2 + 3.0f * f3;
-  const float b1 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
-  a1 = f2 - 2.0f * f3 + f4;
-  a2 = f2 - f4;
-  const float b2 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
-  a1 = f3 - 2.0f * f4 + f5;
-  a2 = 3.0f * f3 - 4.0f * f4 + f5;
-  const float b3 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
-  const float e1 = eps + b1, e2 = eps + b2, e3 = eps + b3;
-  const float mn = fminf(e1, fminf(e2, e3));
-  const float r1 = __fdividef(mn, e1), r2 = __fdividef(mn, e2), r3 = __fdividef(mn, e3);
-  const float w1 = 0.1f * r1 * r1, w2 = 0.6f * r2 * r2, w3 = 0.3f * r3 * r3;
-  const float p1 = (1.0f / 3.0f) * f1 + (-7.0f / 6.0f) * f2 + (11.0f / 6.0f) * f3;
-  const float p2 = (-1.0f / 6.0f) * f2 + (5.0f / 6.0f) * f3 + (1.0f / 3.0f) * f4;
-  const float p3 = (1.0f / 3.0f) * f3 + (5.0f / 6.0f) * f4 + (-1.0f / 6.0f) * f5;
-  return __fdividef(w1 * p1 + w2 * p2 + w3 * p3, w1 + w2 + w3);
-}
-
-// The linear 5th-order upwind reconstruction: WENO5 with the optimal weights
-// d = (0.1, 0.6, 0.3), i.e. (2 f1 - 13 f2 + 47 f3 + 27 f4 - 3 f5) / 60.
-__device__ __forceinline__ float upwind5_f(float f1, float f2, float f3, float f4, float f5) {
-  return (1.0f / 30.0f) * f1 + (-13.0f / 60.0f) * f2 + (47.0f / 60.0f) * f3 +
-         (27.0f / 60.0f) * f4 + (-1.0f / 20.0f) * f5;
-}
-
-struct FaceCtx {
-  float rd[3];   // 1/dx, 1/dy, 1/dz
-  float r4d[3];  // 1/(4dx) ...
-  float alpha;
-};
-
-__device__ __forceinline__ FaceCtx make_ctx(const Phys& P, const unsigned long long* red,
-                                            float* maxS) {
-  FaceCtx fc;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    fc.rd[d] = P.rd_f[d];
-    fc.r4d[d] = 0.25f * P.rd_f[d];
-  }
-  fc.alpha = 0.f;
-  *maxS = 0.f;
-  if (P.ceq) {
-    const float maxCh = d2f(fst_unkey(red[1]));
-    fc.alpha = P.dxmag2_f / (maxCh + 1.0e-6f) * P.alpha_f;  // src/cart3d.cpp:285
-    *maxS = d2f(fst_unkey(red[0]));
-  }
-  return fc;
-}
-
-// ---------------------------------------------------------------------------
-// Face terms of one 3D face (normal f) owned by cell index c: G[v], v < nv.
-// ---------------------------------------------------------------------------
-template <int NV, bool HYB>
-__device__ __forceinline__ void face3d(const Geo& g, const Phys& P, const MixedView& M,
-                                       const FaceCtx& fc, long long c, int f, bool smooth,
-                                       int nv, float* G) {
-  const long long sv = g.sv;
-  const long long sf = f == 0 ? 1 : f == 1 ? g.sy : g.sz;
-  const float* un = M.vel + sv * f;
-  const float uf = (-un[c + 2 * sf] + 7.0f * un[c + sf] + 7.0f * un[c] - un[c - sf]) * (1.0f / 12.0f);
-  const bool neg = uf < 0.0f;
-  const long long c0 = neg ? c + 3 * sf : c - 2 * sf;
-  const long long o = neg ? -sf : sf;
-  const float scale = uf * fc.rd[f];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    if (NV == NVMAX && v >= nv) break;
-    const float* q = M.Q + sv * v;
-    const float f1 = __ldg(q + c0), f2 = __ldg(q + c0 + o), f3 = __ldg(q + c0 + 2 * o),
-                f4 = __ldg(q + c0 + 3 * o), f5 = __ldg(q + c0 + 4 * o);
-    const float rec = (HYB && smooth) ? upwind5_f(f1, f2, f3, f4, f5) : weno_f(f1, f2, f3, f4, f5);
-    G[v] = scale * rec;
-  }
-  if (!(P.visc || P.ceq)) return;
-  // velocity gradients at the face: gr[d][w] = d u_w / d x_d (the stress and
-  // C-equation gradient expressions of the reference are the same ones)
-  float gr[3][3];
-#pragma unroll
-  for (int w = 0; w < 3; ++w) {
-    const float* u = M.vel + sv * w;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      if (d == f) {
-        gr[d][w] = (__ldg(u + c + sf) - __ldg(u + c)) * fc.rd[d];
-      } else {
-        const long long st = d == 0 ? 1 : d == 1 ? g.sy : g.sz;
-        gr[d][w] = ((__ldg(u + c + sf + st) + __ldg(u + c + st)) -
-                    (__ldg(u + c + sf - st) + __ldg(u + c - st))) * fc.r4d[d];
-      }
-    }
-  }
-  float V[4] = {0.f, 0.f, 0.f, 0.f};  // x-, y-, z-momentum, energy
-  if (P.visc) {
-    float mu = 0.f;
-    for (int s = 0; s < P.ns; ++s)
-      mu += 0.5f * (__ldg(M.Y + c + sf + sv * s) + __ldg(M.Y + c + sv * s)) * P.mu_f[s];
-    const float div = gr[0][0] + gr[1][1] + gr[2][2];
-    float e = 0.f;
-#pragma unroll
-    for (int w = 0; w < 3; ++w) {
-      // stress components on this face (calculateStressTensor{x,y,z}3dv)
-      const float Tw = (w == f) ? (2.0f / 3.0f) * mu * (3.0f * gr[f][f] - div)
-                                : mu * (gr[f][w] + gr[w][f]);
-      const float* u = M.vel + sv * w;
-      e += 0.5f * (__ldg(u + c + sf) + __ldg(u + c)) * Tw;
-      V[w] += Tw;
-    }
-    V[3] = e;
-  }
-  if (P.ceq) {
-    const float r = 0.5f * (__ldg(M.rho + c) + __ldg(M.rho + c + sf));
-    const float chat = 0.5f * (__ldg(M.C + c + sv) + __ldg(M.C + c + sf + sv));
-    float cn[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q)
-      cn[q] = 0.5f * (__ldg(M.C + c + sv * (2 + q)) + __ldg(M.C + c + sf + sv * (2 + q)));
-    const float cmag = 1.0e-6f + cn[0] * cn[0] + cn[1] * cn[1] + cn[2] * cn[2];
-    const float rc = __fdividef(1.0f, cmag);
-    const float arc = fc.alpha * r * chat;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float base = arc * ((f == d ? 1.0f : 0.0f) - cn[f] * cn[d] * rc);
-#pragma unroll
-      for (int w = 0; w < 3; ++w) V[w] += base * gr[d][w];
-    }
-  }
-#pragma unroll
-  for (int w = 0; w < 4; ++w) G[w] -= V[w] * fc.rd[f];
-}
-
-__device__ __forceinline__ bool smooth_at(const unsigned char* map, long long c, int f) {
-  return map != nullptr && map[c * 3 + f] != 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -413,85 +163,6 @@ __global__ void __launch_bounds__(TX * TY, 3) k_mrhs3d(Geo g, Phys P, MixedView 
   }
 }
 
-// ---------------------------------------------------------------------------
-// 2D face terms of cart2d (src/flux.hpp:23-106, src/viscosity.hpp:25-199,
-// src/ceq.hpp:200-293) with their quirks, in FP32.
-// ---------------------------------------------------------------------------
-template <int NV, bool HYB>
-__device__ __forceinline__ void face2d(const Geo& g, const Phys& P, const MixedView& M,
-                                       const FaceCtx& fc, long long c, int f, bool smooth,
-                                       int nv, float* G) {
-  const long long sv = g.sv, sx = 1, sy = g.sy;
-  const long long sf = f == 0 ? sx : sy;
-  const float* un = M.vel + sv * f;
-  const float uf = (-un[c + 2 * sf] + 7.0f * un[c + sf] + 7.0f * un[c] - un[c - sf]) * (1.0f / 12.0f);
-  const bool neg = uf < 0.0f;
-  const long long c0 = neg ? c + 3 * sf : c - 2 * sf;
-  const long long o = neg ? -sf : sf;
-  const float scale = uf * fc.rd[f];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    if (NV == NVMAX && v >= nv) break;
-    const float* q = M.Q + sv * v;
-    const float f1 = __ldg(q + c0), f2 = __ldg(q + c0 + o), f3 = __ldg(q + c0 + 2 * o),
-                f4 = __ldg(q + c0 + 3 * o), f5 = __ldg(q + c0 + 4 * o);
-    G[v] = scale * ((HYB && smooth) ? upwind5_f(f1, f2, f3, f4, f5) : weno_f(f1, f2, f3, f4, f5));
-  }
-  if (!(P.visc || P.ceq)) return;
-  const float* u = M.vel;
-  const float* v = M.vel + sv;
-  float V[3] = {0.f, 0.f, 0.f};  // x-, y-momentum, energy
-  if (P.visc) {
-    const float mu = P.mu2d_f;
-    float dudx, dvdx, dudy, dvdy;
-    if (f == 0) {
-      dudx = (u[c + sx] - u[c]) * fc.rd[0];
-      dvdx = (v[c + sx] - v[c]) * fc.rd[0];
-      dudy = ((u[c + sy] + u[c + sx + sy]) - (v[c - sy] + u[c + sx - sy])) * fc.r4d[1];  // vel(i,j-1,1)
-      dvdy = ((v[c + sy] + v[c + sx + sy]) - (v[c - sy] + v[c + sx - sy])) * fc.r4d[1];
-    } else {
-      dudx = ((u[c + sx] + u[c + sx + sy]) - (u[c - sx] + u[c - sx + sy])) * fc.r4d[0];
-      dvdx = ((v[c + sx] + v[c + sx + sy]) - (v[c - sx] + v[c - sx + sy])) * fc.r4d[0];
-      dudy = (u[c + sy] - u[c]) * fc.rd[1];
-      dvdy = (v[c + sy] - v[c]) * fc.rd[1];
-    }
-    const float sxx = (2.0f / 3.0f) * mu * (2.0f * dudx - dvdy);
-    const float syy = (2.0f / 3.0f) * mu * (2.0f * dvdy - dudx);
-    const float sxy = mu * (dudy + dvdx);
-    const float sn = f == 0 ? sxx : sxy;  // x-momentum component on this face
-    const float st = f == 0 ? sxy : syy;  // y-momentum component
-    const float q = -P.kheat_f * (M.T[c + sf] - M.T[c]) * fc.rd[f];
-    V[0] = sn;
-    V[1] = st;
-    V[2] = 0.5f * (u[c + sf] + u[c]) * sn + 0.5f * (v[c + sf] + v[c]) * st - q;
-  }
-  if (P.ceq) {
-    const float r = 0.5f * (M.rho[c] + M.rho[c + sf]);
-    const float chat = 0.5f * (M.C[c + sv] + M.C[c + sf + sv]);
-    const float ct0 = 0.5f * (M.C[c + 2 * sv] + M.C[c + sf + 2 * sv]);
-    const float ct1 = 0.5f * (M.C[c + 3 * sv] + M.C[c + sf + 3 * sv]);
-    const float rct = __fdividef(1.0f, ct0 * ct0 + ct1 * ct1 + 1.0e-6f);
-    const float ctf = f == 0 ? ct0 : ct1;
-    const float arc = fc.alpha * r * chat * ctf * rct;
-#pragma unroll
-    for (int w = 0; w < 2; ++w) {
-      const float* vw = M.vel + sv * w;
-      float g0, g1;
-      if (f == 0) {
-        g0 = (vw[c + sx] - vw[c]) * fc.rd[0];
-        g1 = ((vw[c + sy] + vw[c + sx + sy]) - (vw[c - sy] + vw[c + sx - sy])) * fc.r4d[1];
-      } else {
-        g0 = ((vw[c + sx] + vw[c + sx + sy]) - (vw[c - sx] + vw[c - sx + sy])) * fc.r4d[0];
-        g1 = (vw[c + sy] - vw[c]) * fc.rd[1];
-      }
-      V[w] += arc * (ct0 * g0 + ct1 * g1);
-    }
-  }
-  G[0] -= V[0] * fc.rd[f];
-  G[1] -= V[1] * fc.rd[f];
-  G[2] -= V[2] * fc.rd[f];
-}
-
 template <int NV, bool HYB>
 __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
                                                     const unsigned long long* __restrict__ red,
@@ -499,84 +170,7 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
                                                     const double* Uold, double* Unew, double coef,
                                                     double* __restrict__ Rout) {
   __shared__ float sG[TY][TX][NV];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i = g.ng - 1 + blockIdx.x * (TX - 1) + tx;
-  const int j = g.ng - 1 + blockIdx.y * (TY - 1) + ty;
-  const long long sv = g.sv, sy = g.sy;
-  const int nv = P.nv;
-  float maxS;
-  FaceCtx fc = make_ctx(P, red, &maxS);
-  fc.rd[2] = fc.rd[0];
-  const bool fi = i <= g.ngi - g.ng - 1;
-  const bool fj = j <= g.ngj - g.ng - 1;
-  const bool ci = tx >= 1 && i >= g.ng && i < g.ngi - g.ng;
-  const bool cj = ty >= 1 && j >= g.ng && j < g.ngj - g.ng;
-  const long long c = (long long)i + sy * j;
-  float Gx[NV], Gy[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) Gx[v] = Gy[v] = 0.f;
-  if (fi && cj) face2d<NV, HYB>(g, P, M, fc, c, 0, HYB && smooth_at(smap, c, 0), nv, Gx);
-  if (fj && ci) face2d<NV, HYB>(g, P, M, fc, c, 1, HYB && smooth_at(smap, c, 1), nv, Gy);
-#pragma unroll
-  for (int v = 0; v < NV; ++v) sG[ty][tx][v] = Gy[v];
-  __syncthreads();
-  float R[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    const float gxl = __shfl_up_sync(0xffffffffu, Gx[v], 1);
-    R[v] = 0.f;
-    if (ci && cj) R[v] = -((Gx[v] - gxl) + (Gy[v] - sG[ty - 1][tx][v]));
-  }
-  if (!(ci && cj)) return;
-  const double* p = M.p;
-  const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) * P.r12x;
-  const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) * P.r12y;
-  double Rd[3] = {f2d(R[0]) - dpx, f2d(R[1]) - dpy, f2d(R[2])};
-  if (P.buoyancy) {
-    const double rhop = M.rho64[c] - P.rho_ref;
-    if (rhop >= 1e-6 || rhop <= -1e-6) {
-      const double f = -P.g * rhop;
-      const float vb = M.Q[c + sv] / M.Q[c + 3 * sv];  // m_y / rho_1 (reference)
-      Rd[1] += f;
-      Rd[2] += f2d(fabsf(vb)) * f;
-    }
-  }
-  auto emit = [&](int v, double Rv) {
-    if (Rout) Rout[c + sv * v] = Rv;
-    else Unew[c + sv * v] = Uold[c + sv * v] + coef * Rv;
-  };
-#pragma unroll
-  for (int w = 0; w < 3; ++w) emit(w, Rd[w]);
-#pragma unroll
-  for (int v = 3; v < NV; ++v) {
-    if (NV == NVMAX && v >= nv) break;
-    emit(v, f2d(R[v]));
-  }
-  if (P.ceq) {
-    const float r12x = P.r12_f[0], r12y = P.r12_f[1];
-    auto d4 = [&](const float* a, long long st, float r12) {
-      return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
-    };
-    const float dxr = d4(M.rho, 1, r12x), dyr = d4(M.rho, sy, r12y);
-    const float dxe = d4(M.nrg, 1, r12x), dye = d4(M.nrg, sy, r12y);
-    const float divu = d4(M.vel, 1, r12x) + d4(M.vel + sv, sy, r12y);
-    const float rgrad = sqrtf(dxr * dxr + dyr * dyr);
-    const float dnednr = (dxr * dxe + dyr * dye) * (dxr * dxr + dyr * dyr);
-    const bool i1 = dnednr < 0.0f;
-    const float Gs[4] = {(!i1 && divu < 0.f) ? rgrad : 0.f, i1 ? rgrad : 0.f, -dyr, dxr};
-    const float dxm = P.dxmag_f;
-    const float src = maxS / (P.eps_f * dxm);
-    const float dif = P.kap_f * maxS * dxm;
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const float* Cn = M.C + sv * n;
-      const float cc = Cn[c];
-      const float lap = (Cn[c + 1] - 2.0f * cc + Cn[c - 1]) * fc.rd[0] +
-                        (Cn[c + sy] - 2.0f * cc + Cn[c - sy]) * fc.rd[1];
-      emit(nv + n, f2d(src * (Gs[n] - cc) + dif * lap));
-    }
-    emit(nv + 4, 0.0);
-  }
+  rhs2d_tile<NV, HYB, TY>(g, P, M, red, smap, Uold, Unew, coef, Rout, blockIdx.x, blockIdx.y, sG);
 }
 
 // ghost cells of the stage-1 buffer: U1 = U + (0.5*dt)*0 (src/rk.cpp:42-50)

@@ -210,6 +210,38 @@ int fst_kernel_times(fst_ctx* ctx, fst_kernel_time* out, int max, int* count);
 int fst_rhs2d_noalloc(const fst_config* cfg, const double* d_U, double* d_R, size_t n,
                       void* cuda_stream);
 
+/* Batched 2D ensemble: many independent 2D cases of uneven size advanced
+ * together in FST_MODE_MIXED.  Replaces running one cart2d_func per case
+ * (src/main.cpp:40-72 once per deck).  Every case must be 2D, mixed, and
+ * share ns and the visc / ceq / buoyancy switches; grids, spacings, time
+ * steps, gases, gravity and BCs may differ.  Per RK stage the whole ensemble
+ * takes one persistent launch of the fused RHS over a (case, tile) work list;
+ * a time step (preStep BCs + two stages) is one CUDA graph replay. */
+typedef struct fst_batch fst_batch;
+typedef struct fst_batch_info_t {
+  int ncases;
+  int tile_height;        /* threads along j of the RHS tile (4, 8 or 16)  */
+  int tiles;              /* work items per stage                         */
+  int persistent_blocks;  /* blocks of the persistent RHS launch          */
+  int launches_per_step;  /* kernels in the captured step graph           */
+  int reserved;
+  int64_t interior_cells; /* sum over cases                               */
+} fst_batch_info_t;
+int fst_batch_create(const fst_config* cfgs, int ncases, fst_batch** out);
+void fst_batch_destroy(fst_batch* b);
+const char* fst_batch_last_error(const fst_batch* b);
+int fst_batch_set_state(fst_batch* b, int case_index, const double* U, size_t n);
+int fst_batch_get_state(fst_batch* b, int case_index, double* U, size_t n);
+int fst_batch_rk_step(fst_batch* b, int nsteps);
+int fst_batch_synchronize(fst_batch* b);
+void* fst_batch_stream(fst_batch* b);  /* the cudaStream_t the graph runs on */
+int fst_batch_set_tile_height(fst_batch* b, int tile_height);
+int fst_batch_info(const fst_batch* b, fst_batch_info_t* out);
+/* Autotuner: time every tile height on this ensemble (state restored
+ * afterwards) and keep the fastest; with json_path, reuse a stored choice for
+ * the same GPU and ensemble signature unless `force`, and store new ones. */
+int fst_batch_tune(fst_batch* b, const char* json_path, int force);
+
 /* Seeded initial conditions generated on the host (same on every platform;
  * no libm calls).  `kind`: FST_IC_*.  Writes the interior of U (LayoutLeft,
  * n = fst_state_size()); ghosts and C variables are set to zero. */
