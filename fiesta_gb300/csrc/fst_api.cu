@@ -459,6 +459,8 @@ int fst_compute_rhs(fst_ctx* c, double* R, size_t n) {
   }
   int rc = FST_OK;
   if (c->g.ndim == 3) rc = bcs(c, c->Ua);  // cart3d_func::compute applies BCs first
+  c->bm.stage = 0;
+  c->bm.classified = false;
   if (!rc) rc = stage(c, c->Ua, c->Ua, nullptr, 0.0, c->Rdev, false);
   if (rc) return rc;
   if (R) {
@@ -477,10 +479,14 @@ int fst_rk_step(fst_ctx* c, int nsteps) {
     const bool two_d = c->g.ndim == 2;
     if (two_d) rc = bcs(c, c->Ua);  // cart2d_func::preStep
     if (!rc && !two_d) rc = bcs(c, c->Ua);
+    c->bm.stage = 1;
     if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, true);
     if (!rc && !two_d) rc = bcs(c, c->Ub);
+    c->bm.stage = 2;
     if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
     if (rc) return rc;
+    c->bm.step += 1;
+    c->bm.classified = false;
     c->stats.steps += 1;
   }
   cudaEventRecord(c->ev1, c->stream);
@@ -551,6 +557,58 @@ int fst_get_stats(const fst_ctx* cc, fst_stats* out) {
     if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) out->last_step_ms = ms;
   }
   out->flagged_face_fraction = fst_mixed_flagged_fraction(c->bm, c->stream);
+  return FST_OK;
+}
+
+int fst_hybrid_features(fst_ctx* c, float* d_features, unsigned char* d_labels, size_t capacity,
+                        float label_ratio, size_t* count) {
+  if (!c || !d_features || !d_labels || !count) return FST_ERR_INVALID;
+  if (c->cf.mode == FST_MODE_PLAIN_FP64) return fail(c, FST_ERR_UNSUPPORTED, "needs a mixed context");
+  if (!c->bm.ymax) {  // mixed contexts get the hybrid work arrays on first use
+    int rc = fst_hybrid_alloc(c->cf, c->g, c->bm, [&](void** p, size_t bytes) { return alloc(c, p, bytes); });
+    if (rc) return rc;
+  }
+  if (c->g.ndim == 3) {
+    int rc = bcs(c, c->Ua);
+    if (rc) return rc;
+  }
+  c->stats.kernel_launches += fst_mixed_prims(c->g, c->P, c->cf, c->bm, c->Ua, c->stream);
+  const MixedView M{c->bm.Q, c->bm.rho32, c->bm.vel32, c->bm.p64, c->bm.Y, c->bm.nrg, c->bm.C,
+                    c->bm.T32, c->bm.rho64};
+  int rc = fst_hybrid_features_impl(c->g, c->bm, M, d_features, d_labels, capacity, label_ratio,
+                                    count, c->stream);
+  if (rc) return fail(c, rc, "feature kernels");
+  c->stats.kernel_launches += 2;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? FST_OK : cuda_fail(c, e, "features");
+}
+
+int fst_hybrid_set_params(fst_ctx* c, const float* params, float threshold) {
+  if (!c || !params) return FST_ERR_INVALID;
+  if (c->cf.mode != FST_MODE_HYBRID) return fail(c, FST_ERR_UNSUPPORTED, "needs a hybrid context");
+  int rc = fst_hybrid_pack(c->bm, params, c->stream);
+  if (rc) return fail(c, rc, "parameter upload");
+  c->bm.threshold = threshold;
+  c->bm.hyb_active = true;
+  return FST_OK;
+}
+
+int fst_hybrid_get_counts(fst_ctx* c, fst_hybrid_counts* out, int reset) {
+  if (!c || !out) return FST_ERR_INVALID;
+  if (!c->bm.counters) return fail(c, FST_ERR_UNSUPPORTED, "needs a mixed context");
+  unsigned long long h[8] = {0};
+  cudaError_t e = cudaMemcpyAsync(h, c->bm.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "counts");
+  out->faces = (int64_t)h[0];
+  out->weno_faces = (int64_t)h[1];
+  out->audit_faces = (int64_t)h[2];
+  out->audit_nonsmooth = (int64_t)h[3];
+  out->audit_missed = (int64_t)h[4];
+  if (reset) {
+    e = cudaMemsetAsync(c->bm.counters, 0, sizeof(h), c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "counts reset");
+  }
   return FST_OK;
 }
 

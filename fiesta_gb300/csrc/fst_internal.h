@@ -99,7 +99,15 @@ struct MixedBufs {
   // hybrid smoothness classifier
   bool hyb_active;
   unsigned char* smooth;   // [cells][3] 1 = linear upwind on that face
+  float* ymax;             // largest mass fraction per cell
   void* mlp;               // device weights (fst_hybrid.cu)
+  float threshold, label_ratio;
+  int audit_every;
+  // step bookkeeping (set by fst_rk_step): classify at stage 1 (or for a
+  // bare RHS), reuse at stage 2; audit steps run full WENO
+  long long step;
+  int stage;
+  bool classified;
 };
 struct MixedView {
   const float* Q;    // [nv][cells] conserved variables, Q[ndim] = E + p
@@ -115,7 +123,7 @@ struct MixedView {
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);
 int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc);
-int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
+int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs& b,
                     const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
                     bool ghosts, cudaStream_t st, Prof* prof);
 int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const double* U,
@@ -126,4 +134,10 @@ double fst_mixed_flagged_fraction(const MixedBufs& b, cudaStream_t st);
 // fst_hybrid.cu (FST_MODE_HYBRID)
 int fst_hybrid_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc);
 int fst_hybrid_classify(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
-                        cudaStream_t st, Prof* prof, const unsigned char** smooth);
+                        cudaStream_t st, Prof* prof, const unsigned char** smooth, bool audit);
+int fst_hybrid_features_impl(const Geo& g, const MixedBufs& b, const MixedView& M, float* out,
+                             unsigned char* lab, size_t cap, float ratio, size_t* count,
+                             cudaStream_t st);
+int fst_hybrid_pack(MixedBufs& b, const float* h_params, cudaStream_t st);
+int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
+                    const double* U, cudaStream_t st);

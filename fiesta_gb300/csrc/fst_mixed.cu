@@ -249,12 +249,12 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   A((void**)&b.vel, sizeof(double) * n * g.ndim);
   A((void**)&b.T, sizeof(double) * n);
   A((void**)&b.red, sizeof(unsigned long long) * 2);
-  A((void**)&b.counters, sizeof(unsigned long long) * 4);
+  A((void**)&b.counters, sizeof(unsigned long long) * 8);
   if (!rc && cf.mode == FST_MODE_HYBRID) rc = fst_hybrid_alloc(cf, g, b, alloc);
   return rc;
 }
 
-int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
+int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs& b,
                     const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
                     bool ghosts, cudaStream_t st, Prof* prof) {
   int n = 0;
@@ -277,9 +277,19 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, const Mix
                    P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr,
                    P.ceq ? b.red : nullptr));
   }
-  const bool hyb = cf.mode == FST_MODE_HYBRID && b.hyb_active;
-  const unsigned char* smooth = nullptr;
-  if (hyb) n += fst_hybrid_classify(g, P, b, M, st, prof, &smooth);
+  bool hyb = cf.mode == FST_MODE_HYBRID && b.hyb_active;
+  const unsigned char* smooth = b.smooth;
+  if (hyb) {
+    // classify once per time step (stage 1, or a bare RHS evaluation) and
+    // reuse the map at stage 2; audit steps run full WENO5 and only compare
+    // the classifier's decisions with the smoothness labels
+    const bool audit = b.audit_every > 0 && b.stage != 0 && (b.step % b.audit_every) == 0;
+    if (b.stage != 2 || !b.classified) {
+      n += fst_hybrid_classify(g, P, b, M, st, prof, &smooth, audit);
+      b.classified = true;
+    }
+    if (audit) hyb = false;
+  }
   if (hyb)
     FST_LAUNCH(prof, g.ndim == 3 ? "mrhs3d_hybrid" : "mrhs2d_hybrid", st, n,
                dispatch_rhs<true>(g, P, M, b.red, smooth, Uold, Unew, coef, Rout, st));
@@ -309,6 +319,19 @@ int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const d
   *vel = b.vel;
   *T = b.T;
   return n;
+}
+
+int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
+                    const double* U, cudaStream_t st) {
+  (void)cf;
+  const dim3 pg(cdiv(g.ngi, 256), g.ngj, g.ngk);
+  if (g.ndim == 3)
+    k_mprim<3><<<pg, 256, 0, st>>>(g, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, b.Y, b.nrg,
+                                   b.C, nullptr, nullptr);
+  else
+    k_mprim<2><<<pg, 256, 0, st>>>(g, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, b.nrg,
+                                   b.C, b.T32, nullptr);
+  return 1;
 }
 
 double fst_mixed_flagged_fraction(const MixedBufs& b, cudaStream_t st) {

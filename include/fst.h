@@ -242,6 +242,56 @@ int fst_batch_info(const fst_batch* b, fst_batch_info_t* out);
  * the same GPU and ensemble signature unless `force`, and store new ones. */
 int fst_batch_tune(fst_batch* b, const char* json_path, int force);
 
+/* Learned smoothness classifier (FST_MODE_HYBRID).  No counterpart in the
+ * reference, which runs full WENO5 on every face (src/flux.hpp:223-310).
+ *
+ * A 20 -> 32 -> 32 -> 1 MLP (ReLU, ReLU, sigmoid) reads, per face, the five
+ * undivided differences across the 6-cell WENO stencil of density,
+ * pressure, face-normal velocity and the largest mass fraction, each
+ * normalised by the sum of their magnitudes.  Inference runs in BF16 on the
+ * tensor cores with FP32 accumulation; faces with output <= threshold take
+ * the linear optimal-weight 5th-order upwind flux, the rest full WENO5.
+ * Parameters are FP32, FST_MLP_PARAMS of them, packed as W1[32][20], b1[32],
+ * W2[32][32], b2[32], w3[32], b3.
+ * Labels come from WENO5 smoothness indicators: a face is non-smooth when,
+ * for density or pressure on either upwind stencil, max(beta)/min(beta)
+ * exceeds `label_ratio`. */
+#define FST_MLP_IN 20
+#define FST_MLP_HID 32
+#define FST_MLP_PARAMS (FST_MLP_HID * FST_MLP_IN + FST_MLP_HID + FST_MLP_HID * FST_MLP_HID + \
+                        FST_MLP_HID + FST_MLP_HID + 1)
+/* Features (row-major [n][20] FP32, device) and labels (uint8, device) of
+ * every face of the context's current state (3 faces per face index of the
+ * face box); *count receives the number written (<= capacity).  The context
+ * must be FST_MODE_MIXED or FST_MODE_HYBRID. */
+int fst_hybrid_features(fst_ctx* ctx, float* d_features, unsigned char* d_labels,
+                        size_t capacity, float label_ratio, size_t* count);
+/* Loss and gradient of the mean binary cross-entropy (positives weighted by
+ * pos_weight) over n samples, FP32 on the device (d_grad: FST_MLP_PARAMS). */
+int fst_mlp_grad(const float* d_features, const unsigned char* d_labels, size_t n,
+                 const float* d_params, float pos_weight, float* d_grad, float* h_loss,
+                 void* cuda_stream);
+/* One epoch of minibatch Adam over the n samples (sample order as given). */
+int fst_mlp_train_epoch(const float* d_features, const unsigned char* d_labels, size_t n,
+                        float* d_params, float* d_adam_m, float* d_adam_v, int* adam_step,
+                        float lr, float pos_weight, int batch, float* h_mean_loss,
+                        void* cuda_stream);
+/* Classifier output probability per sample: FP32 CUDA-core path
+ * (tensor_cores = 0) or the BF16 tensor-core inference path (1). */
+int fst_mlp_forward(const float* d_features, size_t n, const float* d_params, float* d_out,
+                    int tensor_cores, void* cuda_stream);
+/* Install trained parameters (host FP32) in a hybrid context and set the
+ * routing threshold; until then a hybrid context runs full WENO5. */
+int fst_hybrid_set_params(fst_ctx* ctx, const float* params, float threshold);
+/* Audit counters of a hybrid context: faces classified, faces routed to
+ * WENO, and on audit steps (every fst_config.audit_every steps, run with
+ * full WENO) faces labelled non-smooth and those the classifier would have
+ * sent to the linear flux. */
+typedef struct fst_hybrid_counts {
+  int64_t faces, weno_faces, audit_faces, audit_nonsmooth, audit_missed;
+} fst_hybrid_counts;
+int fst_hybrid_get_counts(fst_ctx* ctx, fst_hybrid_counts* out, int reset);
+
 /* Seeded initial conditions generated on the host (same on every platform;
  * no libm calls).  `kind`: FST_IC_*.  Writes the interior of U (LayoutLeft,
  * n = fst_state_size()); ghosts and C variables are set to zero. */
