@@ -169,7 +169,21 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
     from fiesta_gb300 import abi
     from fiesta_gb300.solver import Solver, lib
     cfg = make_cfg(n, MODES[mode_name], dt)
+    if mode_name == "hybrid":
+        cfg.audit_every = 20    # a full-WENO audit step every 20 steps
+        cfg.classify_every = 4  # the smoothness map is refreshed every 4 steps
     s = Solver(cfg)
+    hyb = None
+    if mode_name == "hybrid":
+        from fiesta_gb300 import hybrid as H
+        from fiesta_gb300.train_classifier import load_params
+        got = load_params()
+        if got is None:
+            raise RuntimeError("fiesta_gb300/classifier_params.json missing: run "
+                               "python -m fiesta_gb300.train_classifier")
+        params, meta = got
+        H.set_params(s, params, meta["threshold"])
+        hyb = meta
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
     s.set_state(U0)
@@ -194,6 +208,18 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
     cells = cfg.nci * cfg.ncj * cfg.nck
     value = cells * steps / (ms / 1e3) / 1e6
     finite = s.check_finite()
+    U_final = s.get_state()  # after warmup + steps, for the accuracy report
+    hybrid_info = None
+    if hyb is not None:
+        from fiesta_gb300 import hybrid as H
+        c = H.counts(s)
+        hybrid_info = {"weno_face_fraction": c["weno_faces"] / max(1, c["faces"]),
+                       "audit_faces": c["audit_faces"],
+                       "audit_nonsmooth": c["audit_nonsmooth"],
+                       "audit_missed": c["audit_missed"],
+                       "classifier": {k: hyb[k] for k in ("threshold", "label_ratio",
+                                                           "train_faces", "val_weno_fraction",
+                                                           "val_miss_rate")}}
 
     # dominant kernel and its live roofline
     top = max(kt.items(), key=lambda kv: kv[1][1]) if kt else None
@@ -229,8 +255,8 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
     e2e_ms = e0.elapsed_time(e1)
     e2e_val = cells * e2e_steps / (max(e2e_ms / 1e3, wall)) / 1e6
     s.close()
-    return {
-        "value": value, "ms_per_step": ms / steps, "gpu_launches": launches,
+    return U_final, {
+        "value": value, "ms_per_step": ms / steps, "gpu_launches": launches, "hybrid": hybrid_info,
         "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
         "roofline": roof, "clocks": clk.summary(), "finite": finite,
         "e2e": {"value": e2e_val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": n_state * 8,
@@ -292,6 +318,39 @@ def run_batch2d(steps, warmup, ncases=64):
             "launches_per_step": info["launches_per_step"],
             "workload": "64 2D RT cases, n log-uniform in [128,1024], 2 species, viscous, "
                         "C-equation, buoyancy; mixed precision; CUDA graph per step"}
+
+
+def accuracy_report(cfg, U0, finals, nsteps):
+    """rel-L2 per conserved field over the interior, after the same steps:
+    mixed and hybrid against the plain FP64 path (bit-identical to the
+    reference's FP64 arithmetic), and hybrid against mixed (full WENO).
+    Fields that start at zero are compared by their increment."""
+    names = ["x-momentum", "y-momentum", "z-momentum", "energy"] + \
+            [f"species{s}" for s in range(cfg.ns)] + ["C", "C_hat", "C_1", "C_2", "C_3"]
+    ng = cfg.ng
+
+    def I(A, v):
+        return A[ng:-ng, ng:-ng, ng:-ng, v]
+
+    def rel(a, b):
+        d = np.linalg.norm((a - b).ravel())
+        nb = np.linalg.norm(b.ravel())
+        return float(d / nb) if nb > 0 else float(d)
+
+    out = {"steps": nsteps}
+    pairs = [(m, "plain") for m in ("mixed", "hybrid") if m in finals and "plain" in finals]
+    if "hybrid" in finals and "mixed" in finals:
+        pairs.append(("hybrid", "mixed"))
+    for a_, b_ in pairs:
+        rows = {}
+        for v, name in enumerate(names):
+            z = I(U0, v)
+            if np.abs(z).max() > 0:
+                rows[name] = rel(I(finals[a_], v), I(finals[b_], v))
+            else:
+                rows[name + " (increment)"] = rel(I(finals[a_], v) - z, I(finals[b_], v) - z)
+        out[f"{a_}_vs_{b_}"] = rows
+    return out
 
 
 def cpu_sample(n_sample=128, steps=1):
@@ -371,9 +430,12 @@ def main():
     S0 = max_wave_speed(cfg0, U0)
     dt = 0.5 * cfg0.dx / S0
     modes = [m.strip() for m in a.modes.split(",") if m.strip()]
-    results = {}
+    results, finals = {}, {}
     for m in modes:
-        results[m] = run_gpu_mode(m, n, a.steps, a.warmup, U0, dt, peak, peak_kind, a.e2e_steps)
+        finals[m], results[m] = run_gpu_mode(m, n, a.steps, a.warmup, U0, dt, peak, peak_kind,
+                                             a.e2e_steps)
+    accuracy = accuracy_report(make_cfg(n, 0, dt), U0, finals, a.warmup + a.steps)
+    del finals
     # replicas only: each rank runs the whole case; whole-job value sums ranks
     head = modes[-1]
     r = results[head]
@@ -401,6 +463,7 @@ def main():
         "e2e": r["e2e"], "gpu_launches": r["gpu_launches"],
         "modes": {m: {k: v for k, v in results[m].items() if k not in ("clocks",)} for m in modes},
         "batch2d": batch,
+        "accuracy": accuracy,
     }
     print(json.dumps(line))
 

@@ -61,7 +61,8 @@ class FstConfig(C.Structure):
         ("bc_zmin", C.c_int), ("bc_zmax", C.c_int),
         ("mode", C.c_int),
         ("audit_every", C.c_int),
-        ("reserved", C.c_int * 8),
+        ("classify_every", C.c_int),
+        ("reserved", C.c_int * 7),
     ]
 
 
@@ -99,7 +100,8 @@ class FstIcParams(C.Structure):
 def make_config(ndim=3, n=(8, 8, 8), L=(1.0, 1.0, 1.0), dt=1e-6, species=None,
                 R=8.314462, visc=False, ceq=False, kap=10.0, eps=0.4, alpha=40.0,
                 buoyancy=False, g=9.81, rho_ref=0.0, periodic=(False, False, False),
-                bcs=("outflow",) * 6, mode=MODE_PLAIN_FP64, audit_every=0, dx=None):
+                bcs=("outflow",) * 6, mode=MODE_PLAIN_FP64, audit_every=0, dx=None,
+                classify_every=1):
     """Build an FstConfig from deck-like arguments.
 
     ``species`` is a list of dicts {gamma, M, mu} as in ``fiesta.species``.
@@ -134,6 +136,7 @@ def make_config(ndim=3, n=(8, 8, 8), L=(1.0, 1.0, 1.0), dt=1e-6, species=None,
     (cfg.bc_xmin, cfg.bc_xmax, cfg.bc_ymin, cfg.bc_ymax, cfg.bc_zmin, cfg.bc_zmax) = b
     cfg.mode = mode
     cfg.audit_every = audit_every
+    cfg.classify_every = classify_every
     return cfg
 
 

@@ -97,6 +97,7 @@ std::string validate(const fst_config* cf) {
   for (int q = 0; q < 6; ++q)
     if (!bc_ok(b[q])) return "unknown boundary condition type";
   if (cf->mode < FST_MODE_PLAIN_FP64 || cf->mode > FST_MODE_HYBRID) return "unknown mode";
+  if (cf->audit_every < 0 || cf->classify_every < 0) return "negative audit / classify period";
   long long ngi = cf->nci + 6LL, ngj = cf->ncj + 6LL, ngk = cf->ndim == 3 ? cf->nck + 6LL : 1;
   if (ngi * ngj * ngk > (1LL << 40)) return "grid too large";
   return "";
@@ -486,7 +487,6 @@ int fst_rk_step(fst_ctx* c, int nsteps) {
     if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
     if (rc) return rc;
     c->bm.step += 1;
-    c->bm.classified = false;
     c->stats.steps += 1;
   }
   cudaEventRecord(c->ev1, c->stream);

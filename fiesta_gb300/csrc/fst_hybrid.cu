@@ -70,7 +70,10 @@ __device__ __forceinline__ void diffs5(const float a[6], float floor_abs, float*
   }
   const float r = __fdividef(1.0f, s);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) out[k] = d[k] * r;
+  for (int k = 0; k < 5; ++k) {
+    const float v = d[k] * r;
+    out[k] = isfinite(v) ? v : 0.f;  // a non-finite state gives no feature signal
+  }
 }
 
 __device__ __forceinline__ void face_features(const Geo& g, const MixedView& M, const float* ymax,
@@ -494,6 +497,7 @@ inline unsigned cdivh(long long a, int b) { return (unsigned)((a + b - 1) / b); 
 int fst_hybrid_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc) {
   b.hyb_active = false;
   b.audit_every = cf.audit_every;
+  b.classify_every = cf.classify_every > 1 ? cf.classify_every : 1;
   int rc = alloc((void**)&b.smooth, (size_t)g.sv * 3);
   if (!rc) rc = alloc((void**)&b.ymax, sizeof(float) * (size_t)g.sv);
   if (!rc) rc = alloc(&b.mlp, sizeof(MlpDev));

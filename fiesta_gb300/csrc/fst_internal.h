@@ -103,6 +103,7 @@ struct MixedBufs {
   void* mlp;               // device weights (fst_hybrid.cu)
   float threshold, label_ratio;
   int audit_every;
+  int classify_every;
   // step bookkeeping (set by fst_rk_step): classify at stage 1 (or for a
   // bare RHS), reuse at stage 2; audit steps run full WENO
   long long step;

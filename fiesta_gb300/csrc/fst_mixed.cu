@@ -284,7 +284,9 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     // reuse the map at stage 2; audit steps run full WENO5 and only compare
     // the classifier's decisions with the smoothness labels
     const bool audit = b.audit_every > 0 && b.stage != 0 && (b.step % b.audit_every) == 0;
-    if (b.stage != 2 || !b.classified) {
+    const bool due = b.stage == 0 || audit || !b.classified ||
+                     (b.stage == 1 && b.step % b.classify_every == 0);
+    if (due) {
       n += fst_hybrid_classify(g, P, b, M, st, prof, &smooth, audit);
       b.classified = true;
     }

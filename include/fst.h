@@ -96,7 +96,8 @@ typedef struct fst_config {
   int bc_xmin, bc_xmax, bc_ymin, bc_ymax, bc_zmin, bc_zmax; /* FST_BC_*     */
   int mode;                  /* FST_MODE_*                                  */
   int audit_every;           /* HYBRID: full-WENO audit step period (0: never) */
-  int reserved[8];           /* zero                                        */
+  int classify_every;        /* HYBRID: steps between classifications (0, 1: every step) */
+  int reserved[7];           /* zero                                        */
 } fst_config;
 
 /* Per-context statistics (fst_stats). */
