@@ -4,7 +4,9 @@ kernels and write fiesta_gb300/classifier_params.json.
 Data: every face of 4 states of each of `--runs` seeded runs (expanding
 high-pressure bubbles, planar shock tubes, Gaussian pressure-kernel mixing,
 smooth random fields; the benchmark's five-species gas) at `--n`^3, labelled
-by WENO5 smoothness-indicator ratios (> `--ratio` means the face needs WENO).
+by WENO5 smoothness-indicator ratios (> `--ratio` means the face needs WENO;
+the default 1.5 keeps the hybrid within ~2e-5 of full WENO5 over 20 steps of
+the 256^3 benchmark case, 20 trades ~3e-4 for another 2% of speed).
 The last run of each kind is held out for validation.
 
     python -m fiesta_gb300.train_classifier [--runs 50] [--n 48] [--epochs 6]
@@ -36,7 +38,7 @@ def main():
     ap.add_argument("--n", type=int, default=48)
     ap.add_argument("--snapshots", type=int, default=4)
     ap.add_argument("--epochs", type=int, default=6)
-    ap.add_argument("--ratio", type=float, default=20.0)
+    ap.add_argument("--ratio", type=float, default=1.5)
     ap.add_argument("--pos-weight", type=float, default=3.0)
     ap.add_argument("--threshold", type=float, default=0.35)
     ap.add_argument("--out", default=PARAMS_JSON)
