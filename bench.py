@@ -74,35 +74,50 @@ def max_wave_speed(cfg, U):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled around the timed region.
+
+    The sampler starts before the warm-up steps and polls every 50 ms; each
+    sample is stamped on arrival, and the summary keeps the samples that fall
+    inside the marked timed window (widened by one polling period on each
+    side, so that a window shorter than the period still holds a sample).
+    """
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []          # (arrival time, csv line)
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)   # the first sample marks a running sampler
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, t_start, t_end):
+        self.window = (t_start, t_end)
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(2 * self.PERIOD_MS / 1e3)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -112,7 +127,10 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        pad = self.PERIOD_MS / 1e3
+        for t, ln in self.lines:
+            if self.window and not (self.window[0] - pad <= t <= self.window[1] + pad):
+                continue
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -127,7 +145,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "period_ms": self.PERIOD_MS}
 
 
 # Algorithmic bytes per launch of each plain-path kernel (FP64 = 8 B): the
@@ -187,20 +205,22 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
     s.set_state(U0)
-    for _ in range(warmup):
-        s.rk_step(1)
-    torch.cuda.synchronize()
-    l0 = s.stats()["kernel_launches"]
-    s.set_profiling(True)
-    s.kernel_times()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler() as clk:
+        for _ in range(warmup):
+            s.rk_step(1)
         torch.cuda.synchronize()
+        l0 = s.stats()["kernel_launches"]
+        s.set_profiling(True)
+        s.kernel_times()
+        torch.cuda.synchronize()
+        t_start = time.perf_counter()
         ev0.record(stream)
         for _ in range(steps):
             s.rk_step(1)
         ev1.record(stream)
         torch.cuda.synchronize()
+        clk.mark(t_start, time.perf_counter())
     ms = ev0.elapsed_time(ev1)
     kt = s.kernel_times()
     s.set_profiling(False)
