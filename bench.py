@@ -148,28 +148,38 @@ class ClockSampler:
                 "samples": len(sm), "period_ms": self.PERIOD_MS}
 
 
-# Algorithmic bytes per launch of each plain-path kernel (FP64 = 8 B): the
-# fields it must read and write once, counted over the cells it covers.
+# Algorithmic bytes per launch of each kernel: the fields it must read and
+# write once, counted over the cells it covers (FP64 = 8 B, FP32 = 4 B).
 def algorithmic_bytes(kernel, cfg):
     nci, ncj, nck, ns = cfg.nci, cfg.ncj, cfg.nck, cfg.ns
     nv = 4 + ns
-    nvt = nv + 5
+    nvt = nv + (5 if cfg.ceq else 0)
     ngi, ngj, ngk = nci + 6, ncj + 6, nck + 6
     allc = ngi * ngj * ngk
     faces = (nci + 1) * (ncj + 1) * (nck + 1)
     inner = nci * ncj * nck
+    visc, ceq, buoy = bool(cfg.visc), bool(cfg.ceq), bool(cfg.buoyancy)
     tab = {
         # plain FP64 kernels (8-byte words)
         "prim3d": 8 * allc * (nv + 1 + 5 + ns + 1),
         "flux3d": 8 * faces * (nv + 4 + 3 * nv),
         "faces3d": 8 * faces * (3 + ns + 1 + 4 + 18 + 27),
         "cell3d": 8 * inner * (3 * nv + 6 + 18 + 27 + 5 + 2 * nvt),
-        # mixed kernels: FP64 state in, FP32 primitives (+ FP64 p) out; the
-        # fused RHS reads the primitives once and the old state, writes the new
-        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + ns + 1 + 5) + 8),
-        "mrhs3d": inner * (4 * (nv + 1 + 3 + ns + 1 + 5) + 8 + 8 * nvt + 8 * nvt),
+        # mixed: FP64 state in, FP32 primitives (+ FP64 p, rho) out
+        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + visc + (7 if ceq else 0)) + 8
+                           + 8 * buoy),
+        # cell terms: p, u, v, w, [rho, e, C0..4], [rho64]; old and new
+        # state of the momenta, energy and C-variables
+        "mcell3d": inner * (8 + 12 + (28 if ceq else 0) + 8 * buoy
+                            + 16 * (4 + (5 if ceq else 0))),
+        # species: Q_s, u, v, w; old and new state of the species
+        "mspec3d": inner * (4 * (ns + 3) + 16 * ns),
+        # momenta + energy faces: Q0..3, u, v, w, [mu], [rho, C1..4]; the
+        # momenta and energy of U_new read and written
+        "mmom3d": inner * (4 * (4 + 3 + visc + (5 if ceq else 0)) + 16 * 4),
     }
-    tab["mrhs3d_hybrid"] = tab["mrhs3d"] + inner * 3
+    tab["mspec3d_hybrid"] = tab["mspec3d"] + inner * 3
+    tab["mmom3d_hybrid"] = tab["mmom3d"] + inner * 3
     return tab.get(kernel)
 
 

@@ -3,7 +3,8 @@
 Translation units and their floating-point contract:
   fst_plain3d.cu, fst_plain2d.cu, fst_bc.cu  --fmad=false: the plain FP64 path
       reproduces the reference's FP64 arithmetic operation for operation
-  fst_mixed.cu, fst_hybrid.cu, fst_batch.cu   FMA on, fast FP32 math
+  fst_mixed.cu, fst_mixed3d.cu, fst_hybrid.cu, fst_batch.cu
+                                              FMA on, fast FP32 math
   fst_api.cu                                  host orchestration
   fst_host.cpp                                host IC generator, g++ with
       -ffp-contract=off so the same seed gives the same bits on x86 and Arm
@@ -28,6 +29,7 @@ UNITS = [
     ("fst_plain2d.cu", ["--fmad=false"]),
     ("fst_bc.cu", ["--fmad=false"]),
     ("fst_mixed.cu", ["--use_fast_math"]),
+    ("fst_mixed3d.cu", ["--use_fast_math"]),
     ("fst_hybrid.cu", ["--use_fast_math"]),
     ("fst_batch.cu", ["--use_fast_math"]),
     ("fst_api.cu", ["--fmad=false"]),

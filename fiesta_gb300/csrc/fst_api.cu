@@ -272,6 +272,18 @@ std::string fst_setup_geo_phys(const fst_config* cfg, Geo& g, Phys& P) {
   return "";
 }
 
+// After a synchronisation: the device error word of the 3D mixed kernels
+// (a TMA wait that ran out), cleared once reported.
+int device_errors(fst_ctx* c) {
+  if (!c->bm.dev_err) return FST_OK;
+  unsigned int h = 0;
+  cudaError_t e = cudaMemcpy(&h, c->bm.dev_err, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(c, e, "device error word");
+  if (!h) return FST_OK;
+  cudaMemset(c->bm.dev_err, 0, sizeof(h));
+  return fail(c, FST_ERR_TIMEOUT, "a shared-memory plane load did not complete in time");
+}
+
 extern "C" {
 
 const char* fst_last_error(const fst_ctx* c) { return c ? c->err.c_str() : "null context"; }
@@ -350,7 +362,10 @@ int fst_create(const fst_config* cfg, fst_ctx** out) {
     if (!rc && cfg->ceq) rc = allocd(c, &b.MF, 8 * cells);
     if (!rc) rc = allocd(c, &b.red, 2);
   } else if (!rc) {
-    rc = fst_mixed_alloc(*cfg, g, c->bm, [&](void** p, size_t bytes) { return alloc(c, p, bytes); });
+    std::string why;
+    rc = fst_mixed_alloc(*cfg, g, c->bm, [&](void** p, size_t bytes) { return alloc(c, p, bytes); },
+                         &why);
+    if (rc && !why.empty()) fail(c, rc, why);
   }
   // zero state like a fresh Kokkos View; zero work arrays so that entries
   // outside each kernel's range read as the reference's zero-initialised ones
@@ -381,6 +396,7 @@ void fst_destroy(fst_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
+  fst_mixed3d_release(c->bm);
   if (c->Rdev) cudaFree(c->Rdev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -402,7 +418,7 @@ int fst_synchronize(fst_ctx* c) {
   if (!c) return FST_ERR_INVALID;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "synchronize");
-  return FST_OK;
+  return device_errors(c);
 }
 
 int fst_set_state(fst_ctx* c, const double* U, size_t n) {
@@ -420,7 +436,7 @@ int fst_get_state(fst_ctx* c, double* U, size_t n) {
   cudaError_t e = cudaMemcpyAsync(U, c->Ua, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "get_state");
-  return FST_OK;
+  return device_errors(c);
 }
 
 int fst_set_state_device(fst_ctx* c, const double* dU, size_t n) {
@@ -535,7 +551,8 @@ int fst_check_finite(fst_ctx* c) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "check_finite");
   c->stats.nonfinite = h;
-  return h ? fail(c, FST_ERR_NONFINITE, "non-finite value in state") : FST_OK;
+  if (h) return fail(c, FST_ERR_NONFINITE, "non-finite value in state");
+  return device_errors(c);
 }
 
 int fst_get_stats(const fst_ctx* cc, fst_stats* out) {
@@ -573,10 +590,10 @@ int fst_hybrid_features(fst_ctx* c, float* d_features, unsigned char* d_labels, 
     if (rc) return rc;
   }
   c->stats.kernel_launches += fst_mixed_prims(c->g, c->P, c->cf, c->bm, c->Ua, c->stream);
-  const MixedView M{c->bm.Q, c->bm.rho32, c->bm.vel32, c->bm.p64, c->bm.Y, c->bm.nrg, c->bm.C,
+  const MixedView M{c->bm.Q, c->bm.rho32, c->bm.vel32, c->bm.p64, c->bm.mu32, c->bm.nrg, c->bm.C,
                     c->bm.T32, c->bm.rho64};
-  int rc = fst_hybrid_features_impl(c->g, c->bm, M, d_features, d_labels, capacity, label_ratio,
-                                    count, c->stream);
+  int rc = fst_hybrid_features_impl(c->bm.gq, c->bm, M, d_features, d_labels, capacity,
+                                    label_ratio, count, c->stream);
   if (rc) return fail(c, rc, "feature kernels");
   c->stats.kernel_launches += 2;
   cudaError_t e = cudaStreamSynchronize(c->stream);

@@ -498,8 +498,9 @@ int fst_hybrid_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst
   b.hyb_active = false;
   b.audit_every = cf.audit_every;
   b.classify_every = cf.classify_every > 1 ? cf.classify_every : 1;
-  int rc = alloc((void**)&b.smooth, (size_t)g.sv * 3);
-  if (!rc) rc = alloc((void**)&b.ymax, sizeof(float) * (size_t)g.sv);
+  (void)g;  // the map and ymax follow the primitive arrays' geometry
+  int rc = alloc((void**)&b.smooth, (size_t)b.gq.sv * 3);
+  if (!rc) rc = alloc((void**)&b.ymax, sizeof(float) * (size_t)b.gq.sv);
   if (!rc) rc = alloc(&b.mlp, sizeof(MlpDev));
   b.threshold = 0.5f;
   b.label_ratio = 20.0f;

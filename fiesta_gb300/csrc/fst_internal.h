@@ -87,9 +87,15 @@ int fst_plain2d_secondary(const Geo& g, const Phys& P, const Plain2DBufs& b, con
                           cudaStream_t st);
 
 // fst_mixed.cu (FST_MODE_MIXED / FST_MODE_HYBRID)
+struct Mixed3DMaps;  // TMA tensor maps of the 3D primitive arrays (fst_mixed3d.cu)
 struct MixedBufs {
-  // FP32 primitives written by the mixed primitive pass
-  float *Q, *rho32, *vel32, *Y, *T32, *nrg, *C;
+  // Geometry of the primitive arrays.  2D: the state's.  3D: rows padded to
+  // a multiple of 4 floats so that every row, plane and field starts on a
+  // 16-byte boundary, as TMA tensor maps require.
+  Geo gq;
+  // FP32 primitives written by the mixed primitive pass; mu32 is the
+  // mixture viscosity sum_s Y_s mu_s of a cell (3D viscous runs)
+  float *Q, *rho32, *vel32, *mu32, *T32, *nrg, *C;
   double* p64;    // FP64 pressure
   double* rho64;  // FP64 density (buoyancy source)
   // FP64 secondary outputs (fst_secondary)
@@ -109,13 +115,17 @@ struct MixedBufs {
   long long step;
   int stage;
   bool classified;
+  // 3D fused kernels: tensor maps (host copy, passed by value at launch)
+  // and the device error word (FST_DEVERR_* bits; a TMA wait that ran out)
+  Mixed3DMaps* maps3d;
+  unsigned int* dev_err;
 };
 struct MixedView {
   const float* Q;    // [nv][cells] conserved variables, Q[ndim] = E + p
   const float* rho;  // [cells]
   const float* vel;  // [ndim][cells]
   const double* p;   // [cells]
-  const float* Y;    // [ns][cells]
+  const float* mu;   // [cells] mixture viscosity (3D viscous)
   const float* nrg;  // [cells]
   const float* C;    // [5][cells]
   const float* T;    // [cells] (2D viscous heat flux)
@@ -123,7 +133,8 @@ struct MixedView {
 };
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);
-int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc);
+int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc,
+                    std::string* why);
 int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs& b,
                     const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
                     bool ghosts, cudaStream_t st, Prof* prof);
@@ -142,3 +153,12 @@ int fst_hybrid_features_impl(const Geo& g, const MixedBufs& b, const MixedView& 
 int fst_hybrid_pack(MixedBufs& b, const float* h_params, cudaStream_t st);
 int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
                     const double* U, cudaStream_t st);
+
+// fst_mixed3d.cu: the 3D mixed/hybrid right-hand side + RK stage (two
+// fused kernels fed by TMA plane loads) and its tensor maps
+Geo fst_prim_geo(const Geo& g);
+int fst_mixed3d_prepare(const Geo& g, MixedBufs& b, std::string* why);
+void fst_mixed3d_release(MixedBufs& b);
+int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
+                    const unsigned char* smooth, const double* Uold, double* Unew, double coef,
+                    double* Rout, cudaStream_t st, Prof* prof, bool hybrid);

@@ -10,45 +10,38 @@
 //   FP32  velocities, WENO5 reconstruction and fluxes, viscous stress,
 //         C-equation terms, the wave-speed and C_hat maxima
 //
-// Two kernels per stage:
-//   k_mprim    all cells: FP64 state -> FP32 primitives (+ FP64 p), and the
-//              C-equation maxima (maxS, maxCh) by warp max + atomicMax
-//   k_mrhs3d   a fused 2.5D stencil.  A 32x8 thread tile marches along k;
-//              thread (tx, ty) owns column (i0-1+tx, j0-1+ty) and computes the
-//              faces at i+1/2, j+1/2, k+1/2 once each.  Every face carries nv
-//              FP32 values G_v = F_v - V_v/d: the WENO flux F_v and, for the
-//              momenta and energy, the viscous stress and C-equation tensor
-//              terms V_v of the reference (applyViscousTerm*, applyCeq), which
-//              have the same (face(i) - face(i-1))/d form as the flux
-//              divergence.  The left x face comes from lane-1 by shuffle, the
-//              lower y face from the row below through shared memory, the
-//              back z face from the previous plane in registers.  The cell
-//              then adds the pressure gradient (FP64), buoyancy and the
-//              C-equation source and writes Unew = Uold + coef*R in FP64.
-//              Face and stress arrays never go to HBM.
-// Kernels are instantiated per variable count so every per-variable array
-// lives in registers.  The equations, quirks included, are the reference's
-// (src/flux.hpp, src/viscosity.hpp, src/ceq3d.hpp, src/ceq.hpp,
-// src/presgrad.hpp, src/buoyancy.hpp); only the arithmetic precision differs.
-// The error against the FP64 oracle is measured by tests/test_gpu_mixed.py.
+// Per stage: k_mprim over all cells (FP64 state -> FP32 primitives + FP64
+// p, and the C-equation maxima maxS, maxCh by warp max + atomicMax), then
+// the fused right-hand side + RK stage: in 3D the two TMA-fed kernels of
+// fst_mixed3d.cu, in 2D k_mrhs2d below (a 32x8 tile of columns; each thread
+// computes the faces at i+1/2 and j+1/2 once, the left x face by shuffle,
+// the lower y face through shared memory; every face carries nv FP32
+// values G_v = F_v - V_v/d: the WENO flux, and for the momenta and energy
+// the viscous and C-equation face terms).  Face and stress arrays never go
+// to HBM.  Kernels are instantiated per variable count so every
+// per-variable array lives in registers.  The equations, quirks included,
+// are the reference's (src/flux.hpp, src/viscosity.hpp, src/ceq.hpp,
+// src/ceq3d.hpp, src/presgrad.hpp, src/buoyancy.hpp); only the arithmetic
+// precision differs.  The error against the FP64 oracle is measured by
+// tests/test_gpu_mixed.py.
 #include "fst_mixed_dev.cuh"
 
 namespace {
 using namespace fstm;
 
 template <int NDIM>
-__global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __restrict__ U,
+__global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const double* __restrict__ U,
                                                float* __restrict__ Q, float* __restrict__ rho,
                                                double* __restrict__ rho64,
                                                float* __restrict__ vel, double* __restrict__ pr,
-                                               float* __restrict__ Y, float* __restrict__ nrg,
+                                               float* __restrict__ mu, float* __restrict__ nrg,
                                                float* __restrict__ Cc, float* __restrict__ T,
                                                unsigned long long* __restrict__ red) {
   // grid: x covers i in blocks of 256, y = j, z = k (no integer division)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float lS = -3.0e38f, lC = -3.0e38f;
   if (i < g.ngi)
-    mprim_cell<NDIM>(g, P, U, Q, rho, rho64, vel, pr, Y, nrg, Cc, T, red != nullptr, i,
+    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, mu, nrg, Cc, T, red != nullptr, i,
                      blockIdx.y, blockIdx.z, lS, lC);
   if (red) {
     lS = warp_maxf(lS);
@@ -57,109 +50,6 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Phys P, const double* __re
       atomicMax(&red[0], fst_key((double)lS));
       atomicMax(&red[1], fst_key((double)lC));
     }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// k_mrhs3d: fused 2.5D RHS + RK stage.  Rout (FP64) instead of the update
-// when computing a bare right-hand side.
-// ---------------------------------------------------------------------------
-template <int NV, bool HYB>
-__global__ void __launch_bounds__(TX * TY, 3) k_mrhs3d(Geo g, Phys P, MixedView M,
-                                                    const unsigned long long* __restrict__ red,
-                                                    const unsigned char* __restrict__ smap,
-                                                    const double* Uold, double* Unew, double coef,
-                                                    double* __restrict__ Rout) {
-  __shared__ float sG[TY][TX][NV];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i = g.ng - 1 + blockIdx.x * (TX - 1) + tx;  // column of this thread
-  const int j = g.ng - 1 + blockIdx.y * (TY - 1) + ty;
-  const int kc0 = g.ng + blockIdx.z * KZ;
-  const int kc1 = min(kc0 + KZ, g.ngk - g.ng);
-  const long long sv = g.sv, sy = g.sy, sz = g.sz;
-  const int nv = P.nv;
-  float maxS;
-  const FaceCtx fc = make_ctx(P, red, &maxS);
-  const bool fi = i <= g.ngi - g.ng - 1;  // x face i+1/2 exists
-  const bool fj = j <= g.ngj - g.ng - 1;  // y face j+1/2 exists
-  const bool ci = tx >= 1 && i >= g.ng && i < g.ngi - g.ng;
-  const bool cj = ty >= 1 && j >= g.ng && j < g.ngj - g.ng;
-  const bool cell_col = ci && cj;
-
-  float Gz[NV], Gx[NV], Gy[NV], Gzn[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) Gz[v] = Gx[v] = Gy[v] = Gzn[v] = 0.f;
-  if (cell_col) {  // prologue: z face at kc0 - 1/2
-    const long long c = (long long)i + sy * j + sz * (kc0 - 1);
-    face3d<NV, HYB>(g, P, M, fc, c, 2, HYB && smooth_at(smap, c, 2), nv, Gz);
-  }
-  for (int k = kc0; k < kc1; ++k) {
-    const long long c = (long long)i + sy * j + sz * k;
-    if (fi && cj) face3d<NV, HYB>(g, P, M, fc, c, 0, HYB && smooth_at(smap, c, 0), nv, Gx);
-    if (fj && ci) face3d<NV, HYB>(g, P, M, fc, c, 1, HYB && smooth_at(smap, c, 1), nv, Gy);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) sG[ty][tx][v] = Gy[v];
-    __syncthreads();
-    if (cell_col) face3d<NV, HYB>(g, P, M, fc, c, 2, HYB && smooth_at(smap, c, 2), nv, Gzn);
-    float R[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      const float gxl = __shfl_up_sync(0xffffffffu, Gx[v], 1);
-      R[v] = 0.f;
-      if (cell_col) R[v] = -((Gx[v] - gxl) + (Gy[v] - sG[ty - 1][tx][v]) + (Gzn[v] - Gz[v]));
-    }
-    if (cell_col) {
-      // pressure gradient in FP64 (reference quirk: z spacing is dy)
-      const double* p = M.p;
-      const double dpx = (p[c - 2] - 8.0 * p[c - 1] + 8.0 * p[c + 1] - p[c + 2]) * P.r12x;
-      const double dpy = (p[c - 2 * sy] - 8.0 * p[c - sy] + 8.0 * p[c + sy] - p[c + 2 * sy]) * P.r12y;
-      const double dpz = (p[c - 2 * sz] - 8.0 * p[c - sz] + 8.0 * p[c + sz] - p[c + 2 * sz]) * P.r12pz;
-      double Rd[4] = {f2d(R[0]) - dpx, f2d(R[1]) - dpy, f2d(R[2]) - dpz, f2d(R[3])};
-      if (P.buoyancy) {
-        const double f = -P.g * (M.rho64[c] - P.rho_ref);
-        Rd[1] += f;
-        Rd[3] += f2d(M.vel[c + sv]) * f;
-      }
-      auto emit = [&](int v, double Rv) {
-        if (Rout) Rout[c + sv * v] = Rv;
-        else Unew[c + sv * v] = Uold[c + sv * v] + coef * Rv;
-      };
-#pragma unroll
-      for (int w = 0; w < 4; ++w) emit(w, Rd[w]);
-#pragma unroll
-      for (int v = 4; v < NV; ++v) {
-        if (NV == NVMAX && v >= nv) break;
-        emit(v, f2d(R[v]));
-      }
-      if (P.ceq) {
-        const float r12x = P.r12_f[0], r12y = P.r12_f[1], r12z = P.r12_f[2];
-        auto d4 = [&](const float* a, long long st, float r12) {
-          return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
-        };
-        const float dxr = d4(M.rho, 1, r12x), dyr = d4(M.rho, sy, r12y), dzr = d4(M.rho, sz, r12z);
-        const float dxe = d4(M.nrg, 1, r12x), dye = d4(M.nrg, sy, r12y), dze = d4(M.nrg, sz, r12z);
-        const float divu = d4(M.vel, 1, r12x) + d4(M.vel + sv, sy, r12y) + d4(M.vel + 2 * sv, sz, r12z);
-        const float rgrad = sqrtf(dxr * dxr + dyr * dyr + dzr * dzr);
-        const float dnednr = (dxr * dxe + dyr * dye + dzr * dze) * (dxr * dxr + dyr * dyr + dzr * dzr);
-        const bool ind = dnednr < 0.0f;
-        const float Gs[5] = {divu < 0.f && !ind ? rgrad : 0.f, ind ? rgrad : 0.f, dxr, dyr, dzr};
-        const float dxm = P.dxmag_f;
-        const float src = maxS / (P.eps_f * dxm);
-        const float dif = P.kap_f * maxS * dxm;
-#pragma unroll
-        for (int n = 0; n < 5; ++n) {
-          const float* Cn = M.C + sv * n;
-          const float cc = Cn[c];
-          const float lap = (Cn[c - 1] - 2.0f * cc + Cn[c + 1]) * fc.rd[0] +
-                            (Cn[c - sy] - 2.0f * cc + Cn[c + sy]) * fc.rd[1] +
-                            (Cn[c - sz] - 2.0f * cc + Cn[c + sz]) * fc.rd[2];
-          emit(nv + n, f2d(src * (Gs[n] - cc) + dif * lap));
-        }
-      }
-    }
-#pragma unroll
-    for (int v = 0; v < NV; ++v) Gz[v] = Gzn[v];
-    __syncthreads();
   }
 }
 
@@ -187,19 +77,14 @@ __global__ void k_mghost(Geo g, const double* __restrict__ Uold, double* __restr
 
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 
-// Launch the fused RHS for a compile-time variable count.
+// Launch the fused 2D RHS for a compile-time variable count.
 template <int NV, bool HYB>
 void launch_rhs(const Geo& g, const Phys& P, const MixedView& M, const unsigned long long* red,
                 const unsigned char* smap, const double* Uold, double* Unew, double coef,
                 double* Rout, cudaStream_t st) {
   const dim3 blk(TX, TY, 1);
-  if (g.ndim == 3) {
-    const dim3 grd(cdiv(g.nci, TX - 1), cdiv(g.ncj, TY - 1), cdiv(g.nck, KZ));
-    k_mrhs3d<NV, HYB><<<grd, blk, 0, st>>>(g, P, M, red, smap, Uold, Unew, coef, Rout);
-  } else {
-    const dim3 grd(cdiv(g.nci, TX - 1), cdiv(g.ncj, TY - 1), 1);
-    k_mrhs2d<NV, HYB><<<grd, blk, 0, st>>>(g, P, M, red, smap, Uold, Unew, coef, Rout);
-  }
+  const dim3 grd(cdiv(g.nci, TX - 1), cdiv(g.ncj, TY - 1), 1);
+  k_mrhs2d<NV, HYB><<<grd, blk, 0, st>>>(g, P, M, red, smap, Uold, Unew, coef, Rout);
 }
 
 template <bool HYB>
@@ -220,15 +105,18 @@ void dispatch_rhs(const Geo& g, const Phys& P, const MixedView& M, const unsigne
 }  // namespace
 
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g) {
-  // floats: Q nv, rho, vel ndim, Y ns, nrg, C 5, T; doubles: p and the
+  // floats: Q nv, rho, vel ndim, mu, nrg, C 5, T; doubles: p, rho and the
   // FP64 secondary outputs (rho, p, vel, T); hybrid: 3 map bytes
-  const size_t fl = g.nv + 1 + g.ndim + g.ns + 1 + 5 + 1;
+  const size_t fl = g.nv + 1 + g.ndim + 1 + 1 + 5 + 1 + 2;
   (void)cf;
   return (fl + 1) / 2 + 1 + (size_t)(g.ndim + 3) + 1;
 }
 
-int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc) {
-  const size_t n = (size_t)g.sv;
+int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc,
+                    std::string* why) {
+  b.gq = fst_prim_geo(g);
+  const size_t n = (size_t)b.gq.sv;  // primitive arrays
+  const size_t ns = (size_t)g.sv;    // FP64 secondary outputs (state layout)
   int rc = 0;
   auto A = [&](void** p, size_t bytes) {
     if (!rc) rc = alloc(p, bytes);
@@ -238,19 +126,21 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   A((void**)&b.vel32, sizeof(float) * n * g.ndim);
   A((void**)&b.p64, sizeof(double) * n);
   if (cf.buoyancy) A((void**)&b.rho64, sizeof(double) * n);
-  if (cf.visc && g.ndim == 3) A((void**)&b.Y, sizeof(float) * n * g.ns);
+  if (cf.visc && g.ndim == 3) A((void**)&b.mu32, sizeof(float) * n);
   if (cf.visc && g.ndim == 2) A((void**)&b.T32, sizeof(float) * n);
   if (cf.ceq) {
     A((void**)&b.nrg, sizeof(float) * n);
     A((void**)&b.C, sizeof(float) * n * 5);
   }
-  A((void**)&b.rho, sizeof(double) * n);
-  A((void**)&b.pr, sizeof(double) * n);
-  A((void**)&b.vel, sizeof(double) * n * g.ndim);
-  A((void**)&b.T, sizeof(double) * n);
+  A((void**)&b.rho, sizeof(double) * ns);
+  A((void**)&b.pr, sizeof(double) * ns);
+  A((void**)&b.vel, sizeof(double) * ns * g.ndim);
+  A((void**)&b.T, sizeof(double) * ns);
   A((void**)&b.red, sizeof(unsigned long long) * 2);
   A((void**)&b.counters, sizeof(unsigned long long) * 8);
+  A((void**)&b.dev_err, sizeof(unsigned int));
   if (!rc && cf.mode == FST_MODE_HYBRID) rc = fst_hybrid_alloc(cf, g, b, alloc);
+  if (!rc) rc = fst_mixed3d_prepare(g, b, why);
   return rc;
 }
 
@@ -262,18 +152,18 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     const unsigned long long init[2] = {FST_KEY_LOWEST, FST_KEY_LOWEST};
     cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
   }
-  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.Y, b.nrg, b.C, b.T32, b.rho64};
+  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.mu32, b.nrg, b.C, b.T32, b.rho64};
   const dim3 pg(cdiv(g.ngi, 256), g.ngj, g.ngk);
   if (g.ndim == 3) {
     FST_LAUNCH(prof, "mprim3d", st, n,
                k_mprim<3><<<pg, 256, 0, st>>>(
-                   g, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, P.visc ? b.Y : nullptr,
-                   P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, nullptr,
-                   P.ceq ? b.red : nullptr));
+                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64,
+                   P.visc ? b.mu32 : nullptr, P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr,
+                   nullptr, P.ceq ? b.red : nullptr));
   } else {
     FST_LAUNCH(prof, "mprim2d", st, n,
                k_mprim<2><<<pg, 256, 0, st>>>(
-                   g, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
+                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
                    P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr,
                    P.ceq ? b.red : nullptr));
   }
@@ -287,16 +177,18 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     const bool due = b.stage == 0 || audit || !b.classified ||
                      (b.stage == 1 && b.step % b.classify_every == 0);
     if (due) {
-      n += fst_hybrid_classify(g, P, b, M, st, prof, &smooth, audit);
+      n += fst_hybrid_classify(b.gq, P, b, M, st, prof, &smooth, audit);
       b.classified = true;
     }
     if (audit) hyb = false;
   }
-  if (hyb)
-    FST_LAUNCH(prof, g.ndim == 3 ? "mrhs3d_hybrid" : "mrhs2d_hybrid", st, n,
+  if (g.ndim == 3)
+    n += fst_mixed3d_rhs(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, prof, hyb);
+  else if (hyb)
+    FST_LAUNCH(prof, "mrhs2d_hybrid", st, n,
                dispatch_rhs<true>(g, P, M, b.red, smooth, Uold, Unew, coef, Rout, st));
   else
-    FST_LAUNCH(prof, g.ndim == 3 ? "mrhs3d" : "mrhs2d", st, n,
+    FST_LAUNCH(prof, "mrhs2d", st, n,
                dispatch_rhs<false>(g, P, M, b.red, nullptr, Uold, Unew, coef, Rout, st));
   if (ghosts && !Rout)
     FST_LAUNCH(prof, "mghost", st, n, k_mghost<<<pg, 256, 0, st>>>(g, Uold, Unew));
@@ -328,11 +220,11 @@ int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const Mix
   (void)cf;
   const dim3 pg(cdiv(g.ngi, 256), g.ngj, g.ngk);
   if (g.ndim == 3)
-    k_mprim<3><<<pg, 256, 0, st>>>(g, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, b.Y, b.nrg,
-                                   b.C, nullptr, nullptr);
+    k_mprim<3><<<pg, 256, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, b.mu32,
+                                   b.nrg, b.C, nullptr, nullptr);
   else
-    k_mprim<2><<<pg, 256, 0, st>>>(g, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, b.nrg,
-                                   b.C, b.T32, nullptr);
+    k_mprim<2><<<pg, 256, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
+                                   b.nrg, b.C, b.T32, nullptr);
   return 1;
 }
 

@@ -55,19 +55,23 @@ __device__ __forceinline__ float warp_maxf(float v) {
   return v;
 }
 
-// One cell of the primitive pass.  lS / lC accumulate the interior maxima of
-// the wave speed and |C_hat| when `red` is set (reduced by the caller).
+// One cell of the primitive pass: state index from g, primitive index from
+// gq (the primitive arrays' geometry; equal to g in 2D).  lS / lC
+// accumulate the interior maxima of the wave speed and |C_hat| when `red`
+// is set (reduced by the caller).  mu (3D viscous) receives the mixture
+// viscosity sum_s Y_s mu_s.
 template <int NDIM>
-__device__ __forceinline__ void mprim_cell(const Geo& g, const Phys& P,
+__device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Phys& P,
                                            const double* __restrict__ U, float* __restrict__ Q,
                                            float* __restrict__ rho, double* __restrict__ rho64,
                                            float* __restrict__ vel, double* __restrict__ pr,
-                                           float* __restrict__ Y, float* __restrict__ nrg,
+                                           float* __restrict__ mu, float* __restrict__ nrg,
                                            float* __restrict__ Cc, float* __restrict__ T, bool red,
                                            int i, int j, int k, float& lS, float& lC) {
-  const long long sv = g.sv;
+  const long long sv = g.sv, qv = gq.sv;
   {
     const long long c = (long long)i + g.sy * j + g.sz * k;
+    const long long q = (long long)i + gq.sy * j + gq.sz * k;
     const int s0 = NDIM + 1;  // first species index
     // mixture EOS in FP64 (calculateRhoPT, src/secondary.hpp:60-151):
     // gamma - 1 = R_mix / Cv = (sum rho_s R_s) / (sum rho_s cv_s)
@@ -81,7 +85,7 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Phys& P,
     const double ri = rcp64(r);
     const double gm1 = sRm * rcp64(sCv);
     const float rif = d2f(ri);
-    float Cv2 = 0.f, Cp2 = 0.f;
+    float Cv2 = 0.f, Cp2 = 0.f, m = 0.f;
     for (int s = 0; s < P.ns; ++s) {
       const float rs = d2f(U[c + sv * (s0 + s)]);
       const float ys = rs * rif;
@@ -89,32 +93,33 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Phys& P,
         Cv2 += ys * P.cv2_f[s];
         Cp2 += ys * P.cp2_f[s];
       }
-      if (Y) Y[c + sv * s] = ys;
-      Q[c + sv * (s0 + s)] = rs;
+      m += ys * P.mu_f[s];
+      Q[q + qv * (s0 + s)] = rs;
     }
+    if (mu) mu[q] = m;
     double msq = 0.0;
     float usq = 0.f;
 #pragma unroll
     for (int d = 0; d < NDIM; ++d) {
-      const double m = U[c + sv * d];
-      msq = fma(m, m, msq);
-      const float mf = d2f(m);
+      const double mom = U[c + sv * d];
+      msq = fma(mom, mom, msq);
+      const float mf = d2f(mom);
       const float u = mf * rif;
       usq += u * u;
-      vel[c + sv * d] = u;
-      Q[c + sv * d] = mf;
+      vel[q + qv * d] = u;
+      Q[q + qv * d] = mf;
     }
     const double E = U[c + sv * NDIM];
     const double p = gm1 * (E - 0.5 * msq * ri);  // FP64 pressure recovery
-    pr[c] = p;
-    Q[c + sv * NDIM] = d2f(E + p);
+    pr[q] = p;
+    Q[q + qv * NDIM] = d2f(E + p);
     const float rf = d2f(r);
-    rho[c] = rf;
-    if (rho64) rho64[c] = r;
-    if (T) T[c] = d2f(p) * rif / d2f(sRm * ri);
-    if (nrg) nrg[c] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
+    rho[q] = rf;
+    if (rho64) rho64[q] = r;
+    if (T) T[q] = d2f(p) * rif / d2f(sRm * ri);
+    if (nrg) nrg[q] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
     if (Cc)
-      for (int n = 0; n < 5; ++n) Cc[c + sv * n] = d2f(U[c + sv * (P.nv + n)]);
+      for (int n = 0; n < 5; ++n) Cc[q + qv * n] = d2f(U[c + sv * (P.nv + n)]);
     if (red) {
       const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
                       (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
@@ -124,7 +129,7 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Phys& P,
         if (NDIM == 3) s = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
         else s = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
         lS = fmaxf(lS, s);
-        lC = fmaxf(lC, fabsf(Cc[c + sv]));
+        lC = fmaxf(lC, fabsf(Cc[q + qv]));
       }
     }
   }
@@ -184,87 +189,6 @@ __device__ __forceinline__ FaceCtx make_ctx(const Phys& P, const unsigned long l
     *maxS = d2f(fst_unkey(red[0]));
   }
   return fc;
-}
-
-// ---------------------------------------------------------------------------
-// Face terms of one 3D face (normal f) owned by cell index c: G[v], v < nv.
-// ---------------------------------------------------------------------------
-template <int NV, bool HYB>
-__device__ __forceinline__ void face3d(const Geo& g, const Phys& P, const MixedView& M,
-                                       const FaceCtx& fc, long long c, int f, bool smooth,
-                                       int nv, float* G) {
-  const long long sv = g.sv;
-  const long long sf = f == 0 ? 1 : f == 1 ? g.sy : g.sz;
-  const float* un = M.vel + sv * f;
-  const float uf = (-un[c + 2 * sf] + 7.0f * un[c + sf] + 7.0f * un[c] - un[c - sf]) * (1.0f / 12.0f);
-  const bool neg = uf < 0.0f;
-  const long long c0 = neg ? c + 3 * sf : c - 2 * sf;
-  const long long o = neg ? -sf : sf;
-  const float scale = uf * fc.rd[f];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    if (NV == NVMAX && v >= nv) break;
-    const float* q = M.Q + sv * v;
-    const float f1 = __ldg(q + c0), f2 = __ldg(q + c0 + o), f3 = __ldg(q + c0 + 2 * o),
-                f4 = __ldg(q + c0 + 3 * o), f5 = __ldg(q + c0 + 4 * o);
-    const float rec = (HYB && smooth) ? upwind5_f(f1, f2, f3, f4, f5) : weno_f(f1, f2, f3, f4, f5);
-    G[v] = scale * rec;
-  }
-  if (!(P.visc || P.ceq)) return;
-  // velocity gradients at the face: gr[d][w] = d u_w / d x_d (the stress and
-  // C-equation gradient expressions of the reference are the same ones)
-  float gr[3][3];
-#pragma unroll
-  for (int w = 0; w < 3; ++w) {
-    const float* u = M.vel + sv * w;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      if (d == f) {
-        gr[d][w] = (__ldg(u + c + sf) - __ldg(u + c)) * fc.rd[d];
-      } else {
-        const long long st = d == 0 ? 1 : d == 1 ? g.sy : g.sz;
-        gr[d][w] = ((__ldg(u + c + sf + st) + __ldg(u + c + st)) -
-                    (__ldg(u + c + sf - st) + __ldg(u + c - st))) * fc.r4d[d];
-      }
-    }
-  }
-  float V[4] = {0.f, 0.f, 0.f, 0.f};  // x-, y-, z-momentum, energy
-  if (P.visc) {
-    float mu = 0.f;
-    for (int s = 0; s < P.ns; ++s)
-      mu += 0.5f * (__ldg(M.Y + c + sf + sv * s) + __ldg(M.Y + c + sv * s)) * P.mu_f[s];
-    const float div = gr[0][0] + gr[1][1] + gr[2][2];
-    float e = 0.f;
-#pragma unroll
-    for (int w = 0; w < 3; ++w) {
-      // stress components on this face (calculateStressTensor{x,y,z}3dv)
-      const float Tw = (w == f) ? (2.0f / 3.0f) * mu * (3.0f * gr[f][f] - div)
-                                : mu * (gr[f][w] + gr[w][f]);
-      const float* u = M.vel + sv * w;
-      e += 0.5f * (__ldg(u + c + sf) + __ldg(u + c)) * Tw;
-      V[w] += Tw;
-    }
-    V[3] = e;
-  }
-  if (P.ceq) {
-    const float r = 0.5f * (__ldg(M.rho + c) + __ldg(M.rho + c + sf));
-    const float chat = 0.5f * (__ldg(M.C + c + sv) + __ldg(M.C + c + sf + sv));
-    float cn[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q)
-      cn[q] = 0.5f * (__ldg(M.C + c + sv * (2 + q)) + __ldg(M.C + c + sf + sv * (2 + q)));
-    const float cmag = 1.0e-6f + cn[0] * cn[0] + cn[1] * cn[1] + cn[2] * cn[2];
-    const float rc = __fdividef(1.0f, cmag);
-    const float arc = fc.alpha * r * chat;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float base = arc * ((f == d ? 1.0f : 0.0f) - cn[f] * cn[d] * rc);
-#pragma unroll
-      for (int w = 0; w < 3; ++w) V[w] += base * gr[d][w];
-    }
-  }
-#pragma unroll
-  for (int w = 0; w < 4; ++w) G[w] -= V[w] * fc.rd[f];
 }
 
 __device__ __forceinline__ bool smooth_at(const unsigned char* map, long long c, int f) {

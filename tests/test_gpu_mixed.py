@@ -127,3 +127,23 @@ def test_mixed_many_species_fallback():
     U, Ur = run_pair(cfg, U0, 5)
     for v, st, inc in field_errors(cfg, U, Ur, U0):
         assert st <= STATE_TOL, (v, st)
+
+
+@pytest.mark.parametrize("ns,visc,ceq,buoy", [(1, False, False, False), (3, True, False, True),
+                                             (2, False, True, True), (5, True, True, False)])
+def test_mixed_3d_term_combinations_ragged_tiles(ns, visc, ceq, buoy):
+    """Each optional term on and off, ragged tile edges in x, y and z (the
+    3D kernels cover 31x7 columns x 16 planes per block), periodic and
+    hydrostatic boundaries."""
+    sp = SP5[:ns]
+    cfg = abi.make_config(3, (33, 17, 19), dt=1e-7, species=sp, visc=visc, ceq=ceq,
+                          buoyancy=buoy, g=9.81, rho_ref=1.0, periodic=(False, True, False),
+                          bcs=("outflow", "reflective", "outflow", "outflow", "hydrostatic",
+                               "reflective"),
+                          mode=abi.MODE_MIXED)
+    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 11 + ns, p_ambient=1e5, T_ambient=300.0,
+                            nkernels=4)
+    U, Ur = run_pair(cfg, U0, 6)
+    for v, st, inc in field_errors(cfg, U, Ur, U0):
+        assert st <= STATE_TOL, (v, st)
+        assert inc <= INCR_TOL, (v, inc)
