@@ -48,6 +48,7 @@ struct fst_ctx {
   std::vector<void*> allocs;
   std::vector<size_t> alloc_bytes;
   std::string err;
+  unsigned long long* dstat = nullptr;  // fst_status keys
   fst_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
@@ -208,6 +209,44 @@ __global__ void k_nonfinite(const double* __restrict__ U, long long n, int* flag
       *flag = 1;
       return;
     }
+}
+
+// Per-field minimum and maximum over the interior, as statusCheck's Max/Min
+// reductions (src/status.cpp:86-99, 155-235): strict comparisons against
+// the identities -DBL_MAX / +DBL_MAX, so NaN never enters and -inf (+inf)
+// never becomes a maximum (minimum).  Keys: [2f] max, [2f+1] max of -x.
+struct StatusFields {
+  const double* f[FST_MAXV + 6];
+};
+__global__ void __launch_bounds__(256) k_status(Geo g, StatusFields F,
+                                                unsigned long long* __restrict__ keys) {
+  const double* a = F.f[blockIdx.y];
+  const long long ni = g.nci, nj = g.ncj;
+  const long long n = ni * nj * (g.ndim == 3 ? g.nck : 1);
+  double mx = -1.7976931348623157e308, mn = 1.7976931348623157e308;
+  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
+       t += (long long)gridDim.x * 256) {
+    const long long i = t % ni, j = (t / ni) % nj, k = t / (ni * nj);
+    const double v = a[(i + g.ng) + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)];
+    if (v > mx) mx = v;
+    if (v < mn) mn = v;
+  }
+  __shared__ double smx[8], smn[8];
+  mx = fst_warp_max(mx);
+  mn = -fst_warp_max(-mn);
+  if ((threadIdx.x & 31) == 0) {
+    smx[threadIdx.x >> 5] = mx;
+    smn[threadIdx.x >> 5] = mn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) {
+      if (smx[w] > mx) mx = smx[w];
+      if (smn[w] < mn) mn = smn[w];
+    }
+    atomicMax(&keys[2 * blockIdx.y], fst_key(mx));
+    atomicMax(&keys[2 * blockIdx.y + 1], fst_key(-mn));
+  }
 }
 
 int alloc(fst_ctx* c, void** p, size_t bytes) {
@@ -540,6 +579,63 @@ int fst_secondary(fst_ctx* c, double* out, size_t n) {
   return FST_OK;
 }
 
+int fst_status(fst_ctx* c, double* vmin, double* vmax, double* xmin, double* xmax) {
+  if (!c || !vmin || !vmax) return FST_ERR_INVALID;
+  if ((xmin == nullptr) != (xmax == nullptr)) return fail(c, FST_ERR_INVALID, "xmin/xmax");
+  const Geo& g = c->g;
+  const int nx = g.ndim + 3;
+  StatusFields F{};
+  int nf = g.nvt;
+  for (int v = 0; v < g.nvt; ++v) F.f[v] = c->Ua + g.sv * v;
+  if (xmin) {  // fresh secondaries, ordered as varx: velocity, p, T, rho
+    const double *rho, *pr, *vel, *T;
+    if (c->cf.mode != FST_MODE_PLAIN_FP64) {
+      c->stats.kernel_launches +=
+          fst_mixed_secondary(g, c->P, c->bm, c->Ua, c->stream, &rho, &pr, &vel, &T);
+    } else if (g.ndim == 3) {
+      c->stats.kernel_launches += fst_plain3d_secondary(g, c->P, c->b3, c->Ua, c->stream);
+      rho = c->b3.rho; pr = c->b3.pr; vel = c->b3.vel; T = c->b3.T;
+    } else {
+      c->stats.kernel_launches += fst_plain2d_secondary(g, c->P, c->b2, c->Ua, c->stream);
+      rho = c->b2.rho; pr = c->b2.pr; vel = c->b2.vel; T = c->b2.T;
+    }
+    for (int d = 0; d < g.ndim; ++d) F.f[nf++] = vel + g.sv * d;
+    F.f[nf++] = pr;
+    F.f[nf++] = T;
+    F.f[nf++] = rho;
+  }
+  if (!c->dstat) {
+    int rc = allocd(c, &c->dstat, 2 * (size_t)(FST_MAXV + 6));
+    if (rc) return rc;
+  }
+  unsigned long long init[2 * (FST_MAXV + 6)];
+  for (int q = 0; q < 2 * nf; ++q) init[q] = FST_KEY_LOWEST;
+  cudaError_t e = cudaMemcpyAsync(c->dstat, init, sizeof(unsigned long long) * 2 * nf,
+                                  cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "status init");
+  k_status<<<dim3(152, nf), 256, 0, c->stream>>>(g, F, c->dstat);
+  c->stats.kernel_launches += 1;
+  int rc = check_launch(c, "status");
+  if (rc) return rc;
+  unsigned long long h[2 * (FST_MAXV + 6)];
+  e = cudaMemcpyAsync(h, c->dstat, sizeof(unsigned long long) * 2 * nf, cudaMemcpyDeviceToHost,
+                      c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "status");
+  for (int q = 0; q < nf; ++q) {
+    const double mx = fst_unkey(h[2 * q]), mn = -fst_unkey(h[2 * q + 1]);
+    if (q < g.nvt) {
+      vmax[q] = mx;
+      vmin[q] = mn;
+    } else {
+      xmax[q - g.nvt] = mx;
+      xmin[q - g.nvt] = mn;
+    }
+  }
+  (void)nx;
+  return device_errors(c);
+}
+
 int fst_check_finite(fst_ctx* c) {
   if (!c) return FST_ERR_INVALID;
   const long long n = c->g.sv * c->g.nvt;
@@ -590,8 +686,8 @@ int fst_hybrid_features(fst_ctx* c, float* d_features, unsigned char* d_labels, 
     if (rc) return rc;
   }
   c->stats.kernel_launches += fst_mixed_prims(c->g, c->P, c->cf, c->bm, c->Ua, c->stream);
-  const MixedView M{c->bm.Q, c->bm.rho32, c->bm.vel32, c->bm.p64, c->bm.mu32, c->bm.nrg, c->bm.C,
-                    c->bm.T32, c->bm.rho64};
+  const MixedView M{c->bm.Q,   c->bm.rho32, c->bm.vel32, c->bm.p64,   c->bm.mu32, c->bm.nrg,
+                    c->bm.C,   c->bm.T32,   c->bm.rho64, c->bm.p32};
   int rc = fst_hybrid_features_impl(c->bm.gq, c->bm, M, d_features, d_labels, capacity,
                                     label_ratio, count, c->stream);
   if (rc) return fail(c, rc, "feature kernels");

@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) k_bprim(const BCase* __restrict__ cs,
   float lS = -3.0e38f, lC = -3.0e38f;
   if (local < (int)g.sv) {
     const int i = local % g.ngi, j = local / g.ngi;
-    mprim_cell<2>(g, g, Ps[c], use_a ? B.Ua : B.Ub, B.Q, B.rho32, B.rho64, B.vel32, B.p64, nullptr,
+    mprim_cell<2>(g, g, Ps[c], use_a ? B.Ua : B.Ub, B.Q, B.rho32, B.rho64, B.vel32, B.p64, nullptr, nullptr,
                   B.nrg, B.C, B.T32, red, i, j, 0, lS, lC);
   }
   if (red) {

@@ -85,7 +85,7 @@ __device__ __forceinline__ void face_features(const Geo& g, const MixedView& M, 
   for (int k = 0; k < 6; ++k) {
     const long long cc = c + (k - 2) * sf;
     r[k] = __ldg(M.rho + cc);
-    p[k] = d2f(__ldg(M.p + cc));
+    p[k] = M.pp ? __ldg(M.pp + cc) : d2f(__ldg(M.p + cc));
     u[k] = __ldg(un + cc);
     y[k] = __ldg(ymax + cc);
   }
@@ -118,7 +118,7 @@ __device__ __forceinline__ bool face_label(const Geo& g, const MixedView& M, lon
   for (int k = 0; k < 6; ++k) {
     const long long cc = c + (k - 2) * sf;
     r[k] = __ldg(M.rho + cc);
-    p[k] = d2f(__ldg(M.p + cc));
+    p[k] = M.pp ? __ldg(M.pp + cc) : d2f(__ldg(M.p + cc));
   }
   const float q = fmaxf(fmaxf(beta_ratio(r[0], r[1], r[2], r[3], r[4]),
                               beta_ratio(r[5], r[4], r[3], r[2], r[1])),

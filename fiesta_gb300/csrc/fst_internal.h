@@ -96,7 +96,8 @@ struct MixedBufs {
   // FP32 primitives written by the mixed primitive pass; mu32 is the
   // mixture viscosity sum_s Y_s mu_s of a cell (3D viscous runs)
   float *Q, *rho32, *vel32, *mu32, *T32, *nrg, *C;
-  double* p64;    // FP64 pressure
+  double* p64;    // FP64 pressure (2D)
+  float* p32;     // pressure as an FP32 pair: hi [cells], lo [cells] (3D)
   double* rho64;  // FP64 density (buoyancy source)
   // FP64 secondary outputs (fst_secondary)
   double *rho, *pr, *vel, *T;
@@ -124,12 +125,13 @@ struct MixedView {
   const float* Q;    // [nv][cells] conserved variables, Q[ndim] = E + p
   const float* rho;  // [cells]
   const float* vel;  // [ndim][cells]
-  const double* p;   // [cells]
+  const double* p;   // [cells] FP64 pressure (2D)
   const float* mu;   // [cells] mixture viscosity (3D viscous)
   const float* nrg;  // [cells]
   const float* C;    // [5][cells]
   const float* T;    // [cells] (2D viscous heat flux)
   const double* rho64;  // [cells] FP64 density (buoyancy)
+  const float* pp;      // [2][cells] pressure hi + lo (3D)
 };
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);

@@ -34,15 +34,18 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const doub
                                                float* __restrict__ Q, float* __restrict__ rho,
                                                double* __restrict__ rho64,
                                                float* __restrict__ vel, double* __restrict__ pr,
+                                               float* __restrict__ pp,
                                                float* __restrict__ mu, float* __restrict__ nrg,
                                                float* __restrict__ Cc, float* __restrict__ T,
                                                unsigned long long* __restrict__ red) {
-  // grid: x covers i in blocks of 256, y = j, z = k (no integer division)
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // grid: x runs over the cells of one (i, j) plane in storage order, in
+  // blocks of 256 across row ends (streaming, no idle threads), z = k
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  const int j = t / g.ngi, i = t - j * g.ngi;
   float lS = -3.0e38f, lC = -3.0e38f;
-  if (i < g.ngi)
-    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, mu, nrg, Cc, T, red != nullptr, i,
-                     blockIdx.y, blockIdx.z, lS, lC);
+  if (j < g.ngj)
+    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red != nullptr, i, j,
+                     blockIdx.z, lS, lC);
   if (red) {
     lS = warp_maxf(lS);
     lC = warp_maxf(lC);
@@ -63,16 +66,22 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
   rhs2d_tile<NV, HYB, TY>(g, P, M, red, smap, Uold, Unew, coef, Rout, blockIdx.x, blockIdx.y, sG);
 }
 
-// ghost cells of the stage-1 buffer: U1 = U + (0.5*dt)*0 (src/rk.cpp:42-50)
-__global__ void k_mghost(Geo g, const double* __restrict__ Uold, double* __restrict__ Unew) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, k = g.ndim == 3 ? (int)blockIdx.z : g.ng;
-  if (i >= g.ngi) return;
-  const long long c = (long long)i + g.sy * j + g.sz * blockIdx.z;
-  const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
-                  (g.ndim == 2 || (k >= g.ng && k < g.ngk - g.ng));
-  if (in) return;
-  for (int v = 0; v < g.nvt; ++v) Unew[c + g.sv * v] = Uold[c + g.sv * v];
+// ghost cells of the stage-1 buffer: U1 = U + (0.5*dt)*0 (src/rk.cpp:42-50).
+// One 64-thread block per (j, k) row: a row with ghost j or k is copied
+// whole, an interior row only its 2*ng ghost cells in i.
+__global__ void __launch_bounds__(64) k_mghost(Geo g, const double* __restrict__ Uold,
+                                               double* __restrict__ Unew) {
+  const int j = blockIdx.x, k = blockIdx.y;
+  const bool row_in = j >= g.ng && j < g.ngj - g.ng &&
+                      (g.ndim == 2 || (k >= g.ng && k < g.ngk - g.ng));
+  const long long c0 = g.sy * j + g.sz * k;
+  const int n = row_in ? 2 * g.ng : g.ngi;
+  for (int t = threadIdx.x; t < n * g.nvt; t += 64) {
+    const int v = t / n, q = t - v * n;
+    const int i = row_in ? (q < g.ng ? q : g.ngi - 2 * g.ng + q) : q;
+    const long long c = c0 + i + g.sv * v;
+    Unew[c] = Uold[c];
+  }
 }
 
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
@@ -124,7 +133,8 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   A((void**)&b.Q, sizeof(float) * n * g.nv);
   A((void**)&b.rho32, sizeof(float) * n);
   A((void**)&b.vel32, sizeof(float) * n * g.ndim);
-  A((void**)&b.p64, sizeof(double) * n);
+  if (g.ndim == 3) A((void**)&b.p32, sizeof(float) * n * 2);
+  else A((void**)&b.p64, sizeof(double) * n);
   if (cf.buoyancy) A((void**)&b.rho64, sizeof(double) * n);
   if (cf.visc && g.ndim == 3) A((void**)&b.mu32, sizeof(float) * n);
   if (cf.visc && g.ndim == 2) A((void**)&b.T32, sizeof(float) * n);
@@ -152,18 +162,18 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     const unsigned long long init[2] = {FST_KEY_LOWEST, FST_KEY_LOWEST};
     cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
   }
-  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.mu32, b.nrg, b.C, b.T32, b.rho64};
-  const dim3 pg(cdiv(g.ngi, 256), g.ngj, g.ngk);
+  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.mu32, b.nrg, b.C, b.T32, b.rho64, b.p32};
+  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
   if (g.ndim == 3) {
     FST_LAUNCH(prof, "mprim3d", st, n,
-               k_mprim<3><<<pg, 256, 0, st>>>(
-                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64,
+               k_mprim<3><<<qg, qb, 0, st>>>(
+                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
                    P.visc ? b.mu32 : nullptr, P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr,
                    nullptr, P.ceq ? b.red : nullptr));
   } else {
     FST_LAUNCH(prof, "mprim2d", st, n,
-               k_mprim<2><<<pg, 256, 0, st>>>(
-                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
+               k_mprim<2><<<qg, qb, 0, st>>>(
+                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, nullptr,
                    P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr,
                    P.ceq ? b.red : nullptr));
   }
@@ -191,7 +201,8 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     FST_LAUNCH(prof, "mrhs2d", st, n,
                dispatch_rhs<false>(g, P, M, b.red, nullptr, Uold, Unew, coef, Rout, st));
   if (ghosts && !Rout)
-    FST_LAUNCH(prof, "mghost", st, n, k_mghost<<<pg, 256, 0, st>>>(g, Uold, Unew));
+    FST_LAUNCH(prof, "mghost", st, n,
+               k_mghost<<<dim3(g.ngj, g.ngk), 64, 0, st>>>(g, Uold, Unew));
   return n;
 }
 
@@ -218,13 +229,13 @@ int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const d
 int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
                     const double* U, cudaStream_t st) {
   (void)cf;
-  const dim3 pg(cdiv(g.ngi, 256), g.ngj, g.ngk);
+  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
   if (g.ndim == 3)
-    k_mprim<3><<<pg, 256, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, b.mu32,
-                                   b.nrg, b.C, nullptr, nullptr);
+    k_mprim<3><<<qg, qb, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
+                                   b.mu32, b.nrg, b.C, nullptr, nullptr);
   else
-    k_mprim<2><<<pg, 256, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
-                                   b.nrg, b.C, b.T32, nullptr);
+    k_mprim<2><<<qg, qb, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
+                                   nullptr, b.nrg, b.C, b.T32, nullptr);
   return 1;
 }
 

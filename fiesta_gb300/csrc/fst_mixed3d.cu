@@ -56,7 +56,7 @@ struct Mixed3DMaps {
   CUtensorMap mu;   // mixture viscosity
   CUtensorMap c5;   // C-variables 0..4
   CUtensorMap c4;   // C-variables 1..4 (C_hat, C_1..3)
-  CUtensorMap p;    // FP64 pressure
+  CUtensorMap p;    // pressure hi/lo pair (2 FP32 fields)
   int nsc;          // species per k_mspec3d launch
 };
 
@@ -161,7 +161,7 @@ __host__ __device__ inline MomLayout mom_layout(bool visc, bool ceq) {
   return L;
 }
 struct CellLayout {
-  int p, v, rho, nrg, c, size;  // p: FP64 (2 floats per value)
+  int p, v, rho, nrg, c, size;  // p: pressure hi plane then lo plane
   uint32_t bytes;
 };
 __host__ __device__ inline CellLayout cell_layout(bool ceq) {
@@ -227,21 +227,25 @@ __global__ void __launch_bounds__(TX * TY, 2)
     issue(0);
     if (kc0 + 1 < kc1) issue(1);
   }
-  // own-column windows: p, rho, e, w at k-2 .. k+2 (+ next), C at k-1 .. k+1 (+ next)
+  // own-column windows: p (hi, lo), rho, e, w at k-2 .. k+2 (+ next), C at
+  // k-1 .. k+1 (+ next)
   const float* vz = M.vel + 2 * gq.sv;
-  double pw[5], pn = 0.0;
+  const float* plo = M.pp + gq.sv;
+  float ph[5], pl5[5], phn = 0.f, pln = 0.f;
   float rw[5], ew[5], ww[5], cw[5][3], rn = 0.f, en = 0.f, wn = 0.f, cn[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
     const long long o = cq0 + sz * (kc0 - 3 + m);  // planes kc0-3 .. kc0+1, shifted in below
-    pw[m] = cell ? M.p[o] : 0.0;
+    ph[m] = cell ? M.pp[o] : 0.f;
+    pl5[m] = cell ? plo[o] : 0.f;
     ww[m] = cell ? vz[o] : 0.f;
     rw[m] = (cell && ceq) ? M.rho[o] : 0.f;
     ew[m] = (cell && ceq) ? M.nrg[o] : 0.f;
   }
   if (cell) {
     const long long o = cq0 + sz * (kc0 + 2);
-    pn = M.p[o];
+    phn = M.pp[o];
+    pln = plo[o];
     wn = vz[o];
     if (ceq) {
       rn = M.rho[o];
@@ -273,12 +277,14 @@ __global__ void __launch_bounds__(TX * TY, 2)
     // windows -> k-2 .. k+2 (C: k-1 .. k+1); fetch the next planes
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
-      pw[m] = pw[m + 1];
+      ph[m] = ph[m + 1];
+      pl5[m] = pl5[m + 1];
       ww[m] = ww[m + 1];
       rw[m] = rw[m + 1];
       ew[m] = ew[m + 1];
     }
-    pw[4] = pn;
+    ph[4] = phn;
+    pl5[4] = pln;
     ww[4] = wn;
     rw[4] = rn;
     ew[4] = en;
@@ -292,7 +298,8 @@ __global__ void __launch_bounds__(TX * TY, 2)
     for (int w = 0; w < 9; ++w) uo[w] = un[w];
     if (cell && k + 1 < kc1) {
       const long long o = cq0 + sz * (k + 3);
-      pn = M.p[o];
+      phn = M.pp[o];
+      pln = plo[o];
       wn = vz[o];
       if (ceq) {
         rn = M.rho[o];
@@ -305,12 +312,21 @@ __global__ void __launch_bounds__(TX * TY, 2)
     ok = ok && mbar_wait(&bar[b], (uint32_t)((n / NBUF) & 1), err);
     if (cell && ok) {
       const float* tb = tiles + b * L.size;
-      const double* tp = reinterpret_cast<const double*>(tb + L.p) + pl.own;
-      const double dpx = (tp[-2] - 8.0 * tp[-1] + 8.0 * tp[1] - tp[2]) * P.r12x;
-      const double dpy = (tp[-2 * HX] - 8.0 * tp[-HX] + 8.0 * tp[HX] - tp[2 * HX]) * P.r12y;
+      // 4th-order pressure gradient from the hi/lo pair: the differences of
+      // neighbouring pressures are exact in FP32 for the hi parts (close
+      // values) and carry the lo parts, so only the final combination rounds
+      const float* th = tb + L.p + pl.own;
+      const float* tl = th + PL;
+      auto dif = [](float ha, float la, float hb, float lb) { return (ha - hb) + (la - lb); };
+      const float dpx = (8.0f * dif(th[1], tl[1], th[-1], tl[-1]) - dif(th[2], tl[2], th[-2], tl[-2])) *
+                        P.r12_f[0];
+      const float dpy = (8.0f * dif(th[HX], tl[HX], th[-HX], tl[-HX]) -
+                         dif(th[2 * HX], tl[2 * HX], th[-2 * HX], tl[-2 * HX])) *
+                        P.r12_f[1];
       // reference quirk: the z spacing of the pressure gradient is dy
-      const double dpz = (pw[0] - 8.0 * pw[1] + 8.0 * pw[3] - pw[4]) * P.r12pz;
-      double Rd[4] = {-dpx, -dpy, -dpz, 0.0};
+      const float dpz = (8.0f * dif(ph[3], pl5[3], ph[1], pl5[1]) - dif(ph[4], pl5[4], ph[0], pl5[0])) *
+                        P.r12_f[1];
+      double Rd[4] = {-f2d(dpx), -f2d(dpy), -f2d(dpz), 0.0};
       const float* tu = tb + L.v + pl.own;
       if (buoy) {
         const long long cqk = cq0 + sz * k;
@@ -1017,7 +1033,7 @@ int fst_mixed3d_prepare(const Geo& g, MixedBufs& b, std::string* why) {
             make_map(&m->q4, g, gq, b.Q, g.nv, 4, false, why) &&
             make_map(&m->v2, g, gq, b.vel32, 3, 2, false, why) &&
             make_map(&m->v3, g, gq, b.vel32, 3, 3, false, why) &&
-            make_map(&m->p, g, gq, b.p64, 1, 1, true, why);
+            make_map(&m->p, g, gq, b.p32, 2, 2, false, why);
   if (ok && b.rho32) ok = make_map(&m->rho, g, gq, b.rho32, 1, 1, false, why);
   if (ok && b.nrg) ok = make_map(&m->nrg, g, gq, b.nrg, 1, 1, false, why);
   if (ok && b.mu32) ok = make_map(&m->mu, g, gq, b.mu32, 1, 1, false, why);

@@ -60,104 +60,122 @@ __device__ __forceinline__ float warp_maxf(float v) {
 // accumulate the interior maxima of the wave speed and |C_hat| when `red`
 // is set (reduced by the caller).  mu (3D viscous) receives the mixture
 // viscosity sum_s Y_s mu_s.
+//
+// FP64 work is kept to what the pressure needs: the mixture heat capacities
+// (gamma - 1 = sum rho_s R_s / sum rho_s cv_s) and p = (gamma-1)(E - KE).
+// The kinetic energy is formed in FP32: its error (1e-7 KE) is below the
+// FP32 flux error wherever KE matters and negligible where it does not (the
+// near-hydrostatic states whose pressure gradient needs FP64 accuracy).
+// The pressure goes out as FP64 (pr) or as an FP32 pair hi + lo (pp[q],
+// pp[q + qv]) that carries ~48 bits: differences of neighbouring pressures
+// then come out of FP32 arithmetic (hi - hi' is exact for close values).
 template <int NDIM>
 __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Phys& P,
                                            const double* __restrict__ U, float* __restrict__ Q,
                                            float* __restrict__ rho, double* __restrict__ rho64,
                                            float* __restrict__ vel, double* __restrict__ pr,
-                                           float* __restrict__ mu, float* __restrict__ nrg,
-                                           float* __restrict__ Cc, float* __restrict__ T, bool red,
-                                           int i, int j, int k, float& lS, float& lC) {
+                                           float* __restrict__ pp, float* __restrict__ mu,
+                                           float* __restrict__ nrg, float* __restrict__ Cc,
+                                           float* __restrict__ T, bool red, int i, int j, int k,
+                                           float& lS, float& lC) {
   const long long sv = g.sv, qv = gq.sv;
-  {
-    const long long c = (long long)i + g.sy * j + g.sz * k;
-    const long long q = (long long)i + gq.sy * j + gq.sz * k;
-    const int s0 = NDIM + 1;  // first species index
-    // mixture EOS in FP64 (calculateRhoPT, src/secondary.hpp:60-151):
-    // gamma - 1 = R_mix / Cv = (sum rho_s R_s) / (sum rho_s cv_s)
-    double r = 0.0, sCv = 0.0, sRm = 0.0;
-    for (int s = 0; s < P.ns; ++s) {
-      const double rs = U[c + sv * (s0 + s)];
-      r += rs;
-      sCv = fma(rs, P.cv_s[s], sCv);
-      sRm = fma(rs, P.rm_s[s], sRm);
+  const long long c = (long long)i + g.sy * j + g.sz * k;
+  const long long q = (long long)i + gq.sy * j + gq.sz * k;
+  const int s0 = NDIM + 1;  // first species index
+  // mixture EOS (calculateRhoPT, src/secondary.hpp:60-151)
+  double sCv = 0.0, sRm = 0.0, r64 = 0.0;
+  float rf = 0.f;
+  for (int s = 0; s < P.ns; ++s) {
+    const double rs = U[c + sv * (s0 + s)];
+    if (rho64) r64 += rs;
+    sCv = fma(rs, P.cv_s[s], sCv);
+    sRm = fma(rs, P.rm_s[s], sRm);
+    rf += d2f(rs);
+  }
+  const float rif = __frcp_rn(rf);
+  const double gm1 = sRm * rcp64(sCv);
+  float Cv2 = 0.f, Cp2 = 0.f, m = 0.f;
+  for (int s = 0; s < P.ns; ++s) {
+    const float rs = d2f(U[c + sv * (s0 + s)]);
+    const float ys = rs * rif;
+    if (NDIM == 2) {
+      Cv2 += ys * P.cv2_f[s];
+      Cp2 += ys * P.cp2_f[s];
     }
-    const double ri = rcp64(r);
-    const double gm1 = sRm * rcp64(sCv);
-    const float rif = d2f(ri);
-    float Cv2 = 0.f, Cp2 = 0.f, m = 0.f;
-    for (int s = 0; s < P.ns; ++s) {
-      const float rs = d2f(U[c + sv * (s0 + s)]);
-      const float ys = rs * rif;
-      if (NDIM == 2) {
-        Cv2 += ys * P.cv2_f[s];
-        Cp2 += ys * P.cp2_f[s];
-      }
-      m += ys * P.mu_f[s];
-      Q[q + qv * (s0 + s)] = rs;
-    }
-    if (mu) mu[q] = m;
-    double msq = 0.0;
-    float usq = 0.f;
+    m += ys * P.mu_f[s];
+    Q[q + qv * (s0 + s)] = rs;
+  }
+  if (mu) mu[q] = m;
+  float msq = 0.f, usq = 0.f;
 #pragma unroll
-    for (int d = 0; d < NDIM; ++d) {
-      const double mom = U[c + sv * d];
-      msq = fma(mom, mom, msq);
-      const float mf = d2f(mom);
-      const float u = mf * rif;
-      usq += u * u;
-      vel[q + qv * d] = u;
-      Q[q + qv * d] = mf;
-    }
-    const double E = U[c + sv * NDIM];
-    const double p = gm1 * (E - 0.5 * msq * ri);  // FP64 pressure recovery
-    pr[q] = p;
-    Q[q + qv * NDIM] = d2f(E + p);
-    const float rf = d2f(r);
-    rho[q] = rf;
-    if (rho64) rho64[q] = r;
-    if (T) T[q] = d2f(p) * rif / d2f(sRm * ri);
-    if (nrg) nrg[q] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
-    if (Cc)
-      for (int n = 0; n < 5; ++n) Cc[q + qv * n] = d2f(U[c + sv * (P.nv + n)]);
-    if (red) {
-      const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
-                      (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
-      if (in) {
-        const float pf = d2f(p), mf = sqrtf(d2f(msq));
-        float s;
-        if (NDIM == 3) s = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
-        else s = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
-        lS = fmaxf(lS, s);
-        lC = fmaxf(lC, fabsf(Cc[q + qv]));
-      }
+  for (int d = 0; d < NDIM; ++d) {
+    const float mf = d2f(U[c + sv * d]);
+    msq += mf * mf;
+    const float u = mf * rif;
+    usq += u * u;
+    vel[q + qv * d] = u;
+    Q[q + qv * d] = mf;
+  }
+  const double E = U[c + sv * NDIM];
+  const double p = gm1 * (E - f2d(0.5f * msq * rif));  // FP64 pressure recovery
+  if (pr) pr[q] = p;
+  if (pp) {
+    const float ph = d2f(p);
+    pp[q] = ph;
+    pp[q + qv] = d2f(p - f2d(ph));
+  }
+  Q[q + qv * NDIM] = d2f(E + p);
+  rho[q] = rf;
+  if (rho64) rho64[q] = r64;
+  if (T) T[q] = d2f(p) / d2f(sRm);  // p / (rho R_mix), R_mix = sum rho_s R_s / rho
+  if (nrg) nrg[q] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
+  if (Cc)
+    for (int n = 0; n < 5; ++n) Cc[q + qv * n] = d2f(U[c + sv * (P.nv + n)]);
+  if (red) {
+    const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
+                    (NDIM == 2 || (k >= g.ng && k < g.ngk - g.ng));
+    if (in) {
+      const float pf = d2f(p), mf = sqrtf(msq);
+      float sp;
+      if (NDIM == 3) sp = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
+      else sp = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
+      lS = fmaxf(lS, sp);
+      lC = fmaxf(lC, fabsf(Cc[q + qv]));
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// FP32 WENO5-JS with the reference's weights (src/flux.hpp:241-266); the
-// nonlinear weights are scaled by the smallest (eps+beta) so that no square
-// overflows or underflows in FP32 (the normalised weights are unchanged).
+// FP32 WENO5-JS with the reference's weights (src/flux.hpp:241-266),
+// rearranged for fewer operations and less rounding:
+//  - with d_m = f_m - f_{m+1}, every smoothness indicator is
+//    (13/12) a^2 + (1/4) b^2 with a, b short combinations of the d_m; all
+//    three are taken x4 as (13/3) a^2 + b^2 with eps x4, which leaves the
+//    normalised weights unchanged;
+//  - the nonlinear weights are scaled by the smallest (eps+beta), so that no
+//    square overflows or underflows in FP32;
+//  - the candidate polynomials are p_k = f3 + q_k/6 (q_k in the d_m), so the
+//    result is f3 + sum(w_k q_k) / (6 sum w_k): a correction to f3.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float weno_f(float f1, float f2, float f3, float f4, float f5) {
-  const float eps = 1e-6f;
-  float a1 = f1 - 2.0f * f2 + f3, a2 = f1 - 4.0f * f2 + 3.0f * f3;
-  const float b1 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
-  a1 = f2 - 2.0f * f3 + f4;
-  a2 = f2 - f4;
-  const float b2 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
-  a1 = f3 - 2.0f * f4 + f5;
-  a2 = 3.0f * f3 - 4.0f * f4 + f5;
-  const float b3 = (13.0f / 12.0f) * a1 * a1 + 0.25f * a2 * a2;
-  const float e1 = eps + b1, e2 = eps + b2, e3 = eps + b3;
+  const float d1 = f1 - f2, d2 = f2 - f3, d3 = f3 - f4, d4 = f4 - f5;
+  const float c = 13.0f / 3.0f, eps = 4.0e-6f;
+  float a = d1 - d2, b = d1 - 3.0f * d2;  // f1-2f2+f3, f1-4f2+3f3
+  const float e1 = eps + (c * a * a + b * b);
+  a = d2 - d3;                            // f2-2f3+f4
+  b = d2 + d3;                            // f2-f4
+  const float e2 = eps + (c * a * a + b * b);
+  a = d3 - d4;                            // f3-2f4+f5
+  b = 3.0f * d3 - d4;                     // 3f3-4f4+f5
+  const float e3 = eps + (c * a * a + b * b);
   const float mn = fminf(e1, fminf(e2, e3));
   const float r1 = __fdividef(mn, e1), r2 = __fdividef(mn, e2), r3 = __fdividef(mn, e3);
-  const float w1 = 0.1f * r1 * r1, w2 = 0.6f * r2 * r2, w3 = 0.3f * r3 * r3;
-  const float p1 = (1.0f / 3.0f) * f1 + (-7.0f / 6.0f) * f2 + (11.0f / 6.0f) * f3;
-  const float p2 = (-1.0f / 6.0f) * f2 + (5.0f / 6.0f) * f3 + (1.0f / 3.0f) * f4;
-  const float p3 = (1.0f / 3.0f) * f3 + (5.0f / 6.0f) * f4 + (-1.0f / 6.0f) * f5;
-  return __fdividef(w1 * p1 + w2 * p2 + w3 * p3, w1 + w2 + w3);
+  const float s1 = r1 * r1, s2 = r2 * r2, s3 = r3 * r3;
+  // d_k q_k with d = (0.1, 0.6, 0.3): q1 = 2d1-5d2, q2 = -d2-2d3, q3 = d4-4d3
+  const float num = s1 * (0.2f * d1 - 0.5f * d2) + s2 * (-0.6f * d2 - 1.2f * d3) +
+                    s3 * (0.3f * d4 - 1.2f * d3);
+  const float den = 0.6f * s1 + 3.6f * s2 + 1.8f * s3;  // 6 sum d_k s_k
+  return f3 + __fdividef(num, den);
 }
 
 // The linear 5th-order upwind reconstruction: WENO5 with the optimal weights

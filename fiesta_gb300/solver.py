@@ -44,6 +44,8 @@ _EXPORTS = {
     "fst_rk_step": (C.c_int, [C.c_void_p, C.c_int]),
     "fst_secondary": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_check_finite": (C.c_int, [C.c_void_p]),
+    "fst_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                             C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fst_get_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.FstStats)]),
     "fst_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "fst_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(abi.FstKernelTime), C.c_int,
@@ -170,6 +172,21 @@ class Solver:
         self._check(lib().fst_secondary(self._ctx, _dptr(out), out.size), "secondary")
         return out
 
+    def status(self, secondary=True):
+        """Interior (min, max) per state variable and, with ``secondary``,
+        per secondary variable (velocity, p, T, rho), reduced on the device:
+        ``(vmin, vmax, xmin, xmax)`` arrays (the last two None without)."""
+        nvt = self.shape[3]
+        nx = self.cfg.ndim + 3
+        vmin, vmax = np.zeros(nvt), np.zeros(nvt)
+        xmin = np.zeros(nx) if secondary else None
+        xmax = np.zeros(nx) if secondary else None
+        nul = C.POINTER(C.c_double)()
+        self._check(lib().fst_status(self._ctx, _dptr(vmin), _dptr(vmax),
+                                     _dptr(xmin) if secondary else nul,
+                                     _dptr(xmax) if secondary else nul), "status")
+        return vmin, vmax, xmin, xmax
+
     def check_finite(self):
         rc = lib().fst_check_finite(self._ctx)
         if rc == abi.FST_ERR_NONFINITE:
@@ -249,6 +266,39 @@ class Cart3D(_RkFunc):
 
 class Cart2D(_RkFunc):
     ndim = 2
+
+
+def _is_bad(v):
+    """isBad (src/status.cpp:102-107)."""
+    import math
+    return not ((math.isfinite(v) and (v != 0.0 and abs(v) >= 2.2250738585072014e-308 or v == 0.0))
+                and -1.0e200 < v < 1.0e200)
+
+
+def _is_concern(v):
+    """isConcern (src/status.cpp:109-114)."""
+    return v < -1.0e16 or v > 1.0e16
+
+
+def status_report(f, var_names=None, varx_names=None):
+    """The statusCheck table (src/status.cpp:116-253) for a Cart2D/Cart3D or
+    Solver: one line per variable with its interior min and max and a flag,
+    'bad' (non-normal or beyond 1e200), 'concern' (beyond 1e16) or ''."""
+    s = f.solver if hasattr(f, "solver") else f
+    vmin, vmax, xmin, xmax = s.status(secondary=True)
+    nd = s.cfg.ndim
+    var_names = var_names or [f"var{v}" for v in range(len(vmin))]
+    varx_names = varx_names or (["X-Velocity", "Y-Velocity", "Z-Velocity"][:nd]
+                                + ["Pressure", "Temperature", "Total Density"])
+
+    def flag(a):
+        return "bad" if _is_bad(a) else ("concern" if _is_concern(a) else "")
+
+    rows = []
+    for names, lo, hi in ((var_names, vmin, vmax), (varx_names, xmin, xmax)):
+        for n, a, b in zip(names, lo, hi):
+            rows.append((n, float(a), float(b), flag(a), flag(b)))
+    return rows
 
 
 def rkAdvance(cf, f):

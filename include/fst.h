@@ -172,6 +172,14 @@ int fst_secondary(fst_ctx* ctx, double* varx, size_t n);
 /* Scan the state for NaN/Inf (sets stats.nonfinite); FST_ERR_NONFINITE if any. */
 int fst_check_finite(fst_ctx* ctx);
 
+/* Interior minimum and maximum of every state variable (vmin/vmax: nvt
+ * values) and, when xmin/xmax are given, of the secondary variables of
+ * fst_secondary recomputed from the current state (ndim+3 values: velocity,
+ * p, T, rho) -- the reductions of statusCheck (src/status.cpp:116-253),
+ * computed on the device.  As there, NaN is skipped and a variable without
+ * a value above -DBL_MAX (below +DBL_MAX) reports that identity. */
+int fst_status(fst_ctx* ctx, double* vmin, double* vmax, double* xmin, double* xmax);
+
 int fst_get_stats(const fst_ctx* ctx, fst_stats* out);
 
 /* Per-kernel device timing (the reference's per-region fiestaTimer,
