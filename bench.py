@@ -166,7 +166,7 @@ def algorithmic_bytes(kernel, cfg):
         "faces3d": 8 * faces * (3 + ns + 1 + 4 + 18 + 27),
         "cell3d": 8 * inner * (3 * nv + 6 + 18 + 27 + 5 + 2 * nvt),
         # mixed: FP64 state in, FP32 primitives (+ FP64 p, rho) out
-        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + visc + (7 if ceq else 0)) + 8
+        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + visc + (6 if ceq else 0)) + 8
                            + 8 * buoy),
         # cell terms: p, u, v, w, [rho, e, C0..4], [rho64]; old and new
         # state of the momenta, energy and C-variables

@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(TX * TY, 2)
 // k_mspec3d: species [sb, sb+nsk)
 // ---------------------------------------------------------------------------
 template <int NS, bool HYB>
-__global__ void __launch_bounds__(TX * TY, 2)
+__global__ void __launch_bounds__(TX * TY, 3)
     k_mspec3d(const __grid_constant__ Mixed3DMaps maps, Geo g, Geo gq, Phys P, MixedView M,
               const unsigned char* __restrict__ smap, const double* Uold, double* Unew,
               double coef, double* __restrict__ Rout, int sb, int nsk,
@@ -439,8 +439,10 @@ __global__ void __launch_bounds__(TX * TY, 2)
     if (kc0 + 1 < kc1) issue(1);
   }
 
-  // z-window of the own column: species and w at planes k-2 .. k+3
-  float qz[NS][6], qn[NS], wz[6], wn = 0.f;
+  // z-window of the own column: species and w at planes k-2 .. k+3 (the
+  // new plane and the old state are loaded at the top of each iteration and
+  // first used in its second half, after the x/y faces)
+  float qz[NS][6], wz[6];
   const float* vz = M.vel + 2 * gq.sv;
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
@@ -449,17 +451,7 @@ __global__ void __launch_bounds__(TX * TY, 2)
     for (int s = 0; s < NS; ++s) qz[s][m] = (in_arr && s < nsk) ? M.Q[o + gq.sv * (s0 + s)] : 0.f;
     wz[m] = in_arr ? vz[o] : 0.f;
   }
-#pragma unroll
-  for (int s = 0; s < NS; ++s)
-    qn[s] = (in_arr && s < nsk) ? M.Q[cq0 + gq.sv * (s0 + s) + gq.sz * (kc0 + 3)] : 0.f;
-  if (in_arr) wn = vz[cq0 + gq.sz * (kc0 + 3)];
-  double uo[NS], un[NS];
-  auto load_old = [&](int k, double* u) {
-    const long long c = c0 + g.sz * k;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) u[s] = s < nsk ? Uold[c + g.sv * (s0 + s)] : 0.0;
-  };
-  if (cell_col && !Rout) load_old(kc0, un);
+  double uo[NS];
 
   float Gz[NS], Gx[NS], Gy[NS];
 #pragma unroll
@@ -475,27 +467,23 @@ __global__ void __launch_bounds__(TX * TY, 2)
   int k = kc0;
   for (; k < kc1; ++k) {
     const int n = k - kc0, b = n % NBUF;
-    // window -> planes k-2 .. k+3; fetch plane k+4 and the next old state
+    // window -> planes k-2 .. k+3 (plane k+3 <= kc1 + 2 < ngk); old state
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
 #pragma unroll
       for (int s = 0; s < NS; ++s) qz[s][m] = qz[s][m + 1];
       wz[m] = wz[m + 1];
     }
+    if (in_arr) {
+      const long long o = cq0 + gq.sz * (k + 3);
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-      qz[s][5] = qn[s];
-      uo[s] = un[s];
+      for (int s = 0; s < NS; ++s) qz[s][5] = s < nsk ? M.Q[o + gq.sv * (s0 + s)] : 0.f;
+      wz[5] = vz[o];
     }
-    wz[5] = wn;
-    if (k + 1 < kc1) {
-      if (in_arr) {
-        const long long o = cq0 + gq.sz * (k + 4);
+    if (cell_col && !Rout) {
+      const long long c = c0 + g.sz * k;
 #pragma unroll
-        for (int s = 0; s < NS; ++s) qn[s] = s < nsk ? M.Q[o + gq.sv * (s0 + s)] : 0.f;
-        wn = vz[o];
-      }
-      if (cell_col && !Rout) load_old(k + 1, un);
+      for (int s = 0; s < NS; ++s) uo[s] = s < nsk ? Uold[c + g.sv * (s0 + s)] : 0.0;
     }
     ok = ok && mbar_wait(&bar[b], (uint32_t)((n / NBUF) & 1), err);
     const float* tb = tiles + b * L.size;
@@ -710,20 +698,15 @@ __global__ void __launch_bounds__(TX * TY, 2)
     issue_tile(1);  // plane kc0 + 1 <= kc1 <= ngk - 3
   }
 
-  // z-window of the own column: Q0..3 at planes k-2 .. k+3
-  float qz[4][6], qn[4] = {0.f, 0.f, 0.f, 0.f};
+  // z-window of the own column: Q0..3 at planes k-2 .. k+3 (new plane and
+  // the U_new base loaded at the top of each iteration)
+  float qz[4][6];
 #pragma unroll
   for (int m = 0; m < 6; ++m)
 #pragma unroll
     for (int v = 0; v < 4; ++v)
       qz[v][m] = in_arr ? M.Q[cq0 + gq.sv * v + gq.sz * (kc0 - 3 + m)] : 0.f;
-  if (in_arr)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) qn[v] = M.Q[cq0 + gq.sv * v + gq.sz * (kc0 + 3)];
-  double ub[4], ubn[4] = {0.0, 0.0, 0.0, 0.0};
-  if (cell_col)
-#pragma unroll
-    for (int w = 0; w < 4; ++w) ubn[w] = Ub[c0 + g.sz * kc0 + g.sv * w];
+  double ub[4] = {0.0, 0.0, 0.0, 0.0};
 
   // face averages on the z face between planes ka and ka+1 of the own column
   auto zface_scalars = [&](float a_mu, float b_mu, float a_r, float b_r, const float* a_c,
@@ -770,21 +753,14 @@ __global__ void __launch_bounds__(TX * TY, 2)
     for (int m = 0; m < 5; ++m)
 #pragma unroll
       for (int v = 0; v < 4; ++v) qz[v][m] = qz[v][m + 1];
+    if (in_arr) {
+      const long long o = cq0 + gq.sz * (k + 3);  // plane k+3 <= kc1 + 2 < ngk
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      qz[v][5] = qn[v];
-      ub[v] = ubn[v];
+      for (int v = 0; v < 4; ++v) qz[v][5] = M.Q[o + gq.sv * v];
     }
-    if (k + 1 < kc1) {
-      if (in_arr) {
-        const long long o = cq0 + gq.sz * (k + 4);
+    if (cell_col)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) qn[v] = M.Q[o + gq.sv * v];
-      }
-      if (cell_col)
-#pragma unroll
-        for (int w = 0; w < 4; ++w) ubn[w] = Ub[c0 + g.sz * (k + 1) + g.sv * w];
-    }
+      for (int w = 0; w < 4; ++w) ub[w] = Ub[c0 + g.sz * k + g.sv * w];
     ok = ok && wait_tile(n);
     const float* tb = tiles + (n % NBUF) * L.tsize;
     const float *um = vel_at(k - 1), *u0 = vel_at(k), *u1 = vel_at(k + 1);
