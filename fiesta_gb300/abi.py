@@ -97,6 +97,12 @@ class FstIcParams(C.Structure):
     ]
 
 
+class FstNoiseParams(C.Structure):
+    """fst_noise_params: fiesta.noise.{dh, eta, coff, nt, mode}."""
+    _fields_ = [("dh", C.c_double), ("eta", C.c_double), ("coff", C.c_double),
+                ("nt", C.c_int), ("mode", C.c_int), ("reserved", C.c_int * 6)]
+
+
 def make_config(ndim=3, n=(8, 8, 8), L=(1.0, 1.0, 1.0), dt=1e-6, species=None,
                 R=8.314462, visc=False, ceq=False, kap=10.0, eps=0.4, alpha=40.0,
                 buoyancy=False, g=9.81, rho_ref=0.0, periodic=(False, False, False),

@@ -49,6 +49,8 @@ struct fst_ctx {
   std::vector<size_t> alloc_bytes;
   std::string err;
   unsigned long long* dstat = nullptr;  // fst_status keys
+  int* dnoise = nullptr;                 // noise indicator (fst_noise_filter)
+  unsigned long long* dnoise_key = nullptr;
   fst_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
@@ -177,6 +179,8 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
     P.rm_s[s] = P.cp_s[s] - P.cv_s[s];
     P.cv_f[s] = (float)P.cv_s[s];
     P.rm_f[s] = (float)(P.cp_s[s] - P.cv_s[s]);
+    P.cvl_f[s] = (float)(P.cv_s[s] - (double)P.cv_f[s]);
+    P.rml_f[s] = (float)(P.rm_s[s] - (double)P.rm_f[s]);
     P.mu_f[s] = (float)P.mu_s[s];
     P.cv2_f[s] = (float)P.cv2_s[s];
     P.cp2_f[s] = (float)P.cp2_s[s];
@@ -634,6 +638,22 @@ int fst_status(fst_ctx* c, double* vmin, double* vmax, double* xmin, double* xma
   }
   (void)nx;
   return device_errors(c);
+}
+
+int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
+  if (!c || !np) return FST_ERR_INVALID;
+  if (np->nt < 0) return fail(c, FST_ERR_INVALID, "noise nt must be >= 0");
+  const Geo& g = c->g;
+  if (!c->dnoise) {  // zero-initialised like the module's FS3D_I / FS2D_I
+    int rc = allocd(c, &c->dnoise, (size_t)g.sv);
+    if (!rc) rc = allocd(c, &c->dnoise_key, 1);
+    if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(c->dnoise, 0, sizeof(int) * (size_t)g.sv, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "noise init");
+  }
+  c->stats.kernel_launches +=
+      fst_noise_launch(g, c->cf, c->Ua, c->dnoise, c->dnoise_key, *np, c->stream, &c->prof);
+  return check_launch(c, "noise filter");
 }
 
 int fst_check_finite(fst_ctx* c) {

@@ -5,9 +5,10 @@
 // self-copies x, y, z (bc_xPer / bc_yPer / bc_zPer, src/bc.cpp:133-176; the
 // same result as the ordered halo exchange on one rank), then the face fills
 // x-, x+, y-, y+, z-, z+ of bc_gen (src/bc.cpp:33-131), each over the full
-// transverse extent so that edges and corners inherit earlier fills.  Every
-// step is its own launch because later steps read ghosts written by earlier
-// ones.  One thread owns one ghost line and runs the reference's per-line
+// transverse extent so that edges and corners inherit earlier fills.  Axes
+// are separate launches because later axes read ghosts written by earlier
+// ones; the two faces of an axis share a launch when they touch disjoint
+// cells.  One thread owns one ghost line and runs the reference's per-line
 // loop in the reference's order.
 //
 // Built with --fmad=false: the hydrostatic energy extrapolation must round
@@ -28,13 +29,17 @@ __global__ void k_periodic(Geo g, double* __restrict__ U, int axis) {
                        (int)(t / ((long long)na * nb)));
 }
 
-// bc_gen::operator() for one face: thread per transverse (a, b).
-__global__ void k_face(Geo g, double* __restrict__ U, int axis, int side, int type) {
+// bc_gen::operator() for one face: thread per transverse (a, b).  With
+// blockIdx.y = 0/1 one launch fills both faces of an axis: their lines
+// touch disjoint cells when the axis has at least ng interior cells (each
+// side reads only its own ng interior layers and writes its own ghosts).
+__global__ void k_face(Geo g, double* __restrict__ U, int axis, int side, int type, int type_hi) {
   const int na = axis == 0 ? g.ngj : g.ngi;
   const int nb = axis == 2 ? g.ngj : g.ngk;
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)na * nb) return;
-  fstbc::face_line(g, U, axis, side, type, (int)(t % na), (int)(t / na));
+  const int sd = gridDim.y == 2 ? (int)blockIdx.y : side;
+  fstbc::face_line(g, U, axis, sd, sd ? type_hi : type, (int)(t % na), (int)(t / na));
 }
 
 inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -54,12 +59,20 @@ int fst_launch_bcs(const Geo& g, const fst_config& cf, double* U, cudaStream_t s
                k_periodic<<<nblk(na * nb * g.nvt, B), B, 0, stream>>>(g, U, ax));
   }
   const int types[3][2] = {{cf.bc_xmin, cf.bc_xmax}, {cf.bc_ymin, cf.bc_ymax}, {cf.bc_zmin, cf.bc_zmax}};
+  const int ncell[3] = {g.nci, g.ncj, g.nck};
   for (int ax = 0; ax < g.ndim; ++ax) {
     if (per[ax]) continue;
     long long na = ax == 0 ? g.ngj : g.ngi, nb = ax == 2 ? g.ngj : g.ngk;
-    for (int side = 0; side < 2; ++side) {
+    if (ncell[ax] >= g.ng) {  // both faces in one launch
       FST_LAUNCH(prof, "bc_face", stream, launches,
-                 k_face<<<nblk(na * nb, B), B, 0, stream>>>(g, U, ax, side, types[ax][side]));
+                 k_face<<<dim3(nblk(na * nb, B), 2), B, 0, stream>>>(g, U, ax, 0, types[ax][0],
+                                                                    types[ax][1]));
+      continue;
+    }
+    for (int side = 0; side < 2; ++side) {  // x- before x+ (their lines overlap)
+      FST_LAUNCH(prof, "bc_face", stream, launches,
+                 k_face<<<nblk(na * nb, B), B, 0, stream>>>(g, U, ax, side, types[ax][side],
+                                                           types[ax][side]));
     }
   }
   return launches;

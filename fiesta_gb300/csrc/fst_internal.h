@@ -156,6 +156,11 @@ int fst_hybrid_pack(MixedBufs& b, const float* h_params, cudaStream_t st);
 int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
                     const double* U, cudaStream_t st);
 
+// fst_noise.cu: the postStep noise filter on state U
+int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
+                     unsigned long long* key, const fst_noise_params& np, cudaStream_t st,
+                     Prof* prof);
+
 // fst_mixed3d.cu: the 3D mixed/hybrid right-hand side + RK stage (two
 // fused kernels fed by TMA plane loads) and its tensor maps
 Geo fst_prim_geo(const Geo& g);

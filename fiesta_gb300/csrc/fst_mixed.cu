@@ -29,7 +29,7 @@
 namespace {
 using namespace fstm;
 
-template <int NDIM>
+template <int NDIM, int NS>
 __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const double* __restrict__ U,
                                                float* __restrict__ Q, float* __restrict__ rho,
                                                double* __restrict__ rho64,
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const doub
   const int j = t / g.ngi, i = t - j * g.ngi;
   float lS = -3.0e38f, lC = -3.0e38f;
   if (j < g.ngj)
-    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red != nullptr, i, j,
+    mprim_cell<NDIM, NS>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red != nullptr, i, j,
                      blockIdx.z, lS, lC);
   if (red) {
     lS = warp_maxf(lS);
@@ -85,6 +85,25 @@ __global__ void __launch_bounds__(64) k_mghost(Geo g, const double* __restrict__
 }
 
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
+
+// k_mprim for the run's species count (unrolled up to five species)
+template <int NDIM>
+void launch_mprim(const Geo& g, const Geo& gq, const Phys& P, const double* U, float* Q,
+                  float* rho, double* rho64, float* vel, double* pr, float* pp, float* mu,
+                  float* nrg, float* Cc, float* T, unsigned long long* red, cudaStream_t st) {
+  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
+#define FST_MPRIM(NSV) \
+  k_mprim<NDIM, NSV><<<qg, qb, 0, st>>>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red)
+  switch (g.ns) {
+    case 1: FST_MPRIM(1); break;
+    case 2: FST_MPRIM(2); break;
+    case 3: FST_MPRIM(3); break;
+    case 4: FST_MPRIM(4); break;
+    case 5: FST_MPRIM(5); break;
+    default: FST_MPRIM(0); break;
+  }
+#undef FST_MPRIM
+}
 
 // Launch the fused 2D RHS for a compile-time variable count.
 template <int NV, bool HYB>
@@ -163,19 +182,16 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
   }
   const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.mu32, b.nrg, b.C, b.T32, b.rho64, b.p32};
-  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
   if (g.ndim == 3) {
     FST_LAUNCH(prof, "mprim3d", st, n,
-               k_mprim<3><<<qg, qb, 0, st>>>(
-                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
-                   P.visc ? b.mu32 : nullptr, P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr,
-                   nullptr, P.ceq ? b.red : nullptr));
+               launch_mprim<3>(g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
+                               P.visc ? b.mu32 : nullptr, P.ceq ? b.nrg : nullptr,
+                               P.ceq ? b.C : nullptr, nullptr, P.ceq ? b.red : nullptr, st));
   } else {
     FST_LAUNCH(prof, "mprim2d", st, n,
-               k_mprim<2><<<qg, qb, 0, st>>>(
-                   g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, nullptr,
-                   P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr, P.visc ? b.T32 : nullptr,
-                   P.ceq ? b.red : nullptr));
+               launch_mprim<2>(g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
+                               nullptr, P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr,
+                               P.visc ? b.T32 : nullptr, P.ceq ? b.red : nullptr, st));
   }
   bool hyb = cf.mode == FST_MODE_HYBRID && b.hyb_active;
   const unsigned char* smooth = b.smooth;
@@ -229,13 +245,12 @@ int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const d
 int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
                     const double* U, cudaStream_t st) {
   (void)cf;
-  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
   if (g.ndim == 3)
-    k_mprim<3><<<qg, qb, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
-                                   b.mu32, b.nrg, b.C, nullptr, nullptr);
+    launch_mprim<3>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32, b.mu32, b.nrg,
+                    b.C, nullptr, nullptr, st);
   else
-    k_mprim<2><<<qg, qb, 0, st>>>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
-                                   nullptr, b.nrg, b.C, b.T32, nullptr);
+    launch_mprim<2>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, nullptr, b.nrg,
+                    b.C, b.T32, nullptr, st);
   return 1;
 }
 

@@ -21,23 +21,28 @@ constexpr int NVMAX = 4 + FST_MAX_SPECIES;
 // NaN stays NaN; mantissa ties round away from zero.
 __device__ __forceinline__ float d2f(double x) {
   const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
-  const unsigned int sign = hi & 0x80000000u;
+  // the low 9 exponent bits and 23 mantissa bits in one funnel shift, then
+  // the exponent rebiased 1023 -> 127 (exact modulo 2^32 for the normal
+  // range) and the dropped bits rounded
+  unsigned int bits = __funnelshift_l(lo, hi, 3) - (896u << 23);
+  bits += (lo >> 28) & 1u;  // a carry rounds into the exponent
+  // outside the FP32 normal range (selects, no branch: zeros are common)
   const unsigned int ex = (hi >> 20) & 0x7FFu;
-  const int e = (int)ex - 1023 + 127;
-  const unsigned int m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-  const unsigned int r = (lo >> 28) & 1u;
-  unsigned int bits = (((unsigned int)e << 23) | m) + r;  // a carry rounds into the exponent
-  if (e <= 0) bits = 0u;
-  if (e >= 255) bits = (ex == 0x7FFu && ((hi & 0xFFFFFu) | lo)) ? 0x7FC00000u : 0x7F800000u;
-  return __uint_as_float(sign | bits);
+  const unsigned int big = (ex == 0x7FFu && ((hi & 0xFFFFFu) | lo)) ? 0x7FC00000u : 0x7F800000u;
+  bits = ex < 897u ? 0u : bits;
+  bits = ex > 1150u ? big : bits;
+  return __uint_as_float((hi & 0x80000000u) | bits);
 }
 __device__ __forceinline__ double f2d(float x) {
-  const unsigned int f = __float_as_uint(x);
-  const unsigned int sign = f & 0x80000000u, e = (f >> 23) & 0xFFu, m = f & 0x7FFFFFu;
-  unsigned int hi = sign | ((e + 896u) << 20) | (m >> 3);
-  if (e == 0u) hi = sign;                                   // zero (and FP32 denormals)
-  if (e == 255u) hi = sign | 0x7FF00000u | (m >> 3) | (m ? 0x80000u : 0u);  // inf / NaN
-  return __hiloint2double((int)hi, e == 0u ? 0 : (int)(m << 29));
+  const unsigned int f = __float_as_uint(x), a = f & 0x7FFFFFFFu;
+  unsigned int hi = (a >> 3) + (896u << 20), lo = f << 29;  // exponent rebiased 127 -> 1023
+  // zero / FP32 denormal, inf / NaN (selects, no branch)
+  const unsigned int m = a & 0x7FFFFFu;
+  const unsigned int special = 0x7FF00000u | (m >> 3) | (m ? 0x80000u : 0u);
+  hi = a >= 0x7F800000u ? special : hi;
+  hi = a < 0x00800000u ? 0u : hi;
+  lo = a < 0x00800000u ? 0u : lo;
+  return __hiloint2double((int)(hi | (f & 0x80000000u)), (int)lo);
 }
 
 // FP64 reciprocal by one Newton-Raphson step from the correctly rounded FP32
@@ -55,21 +60,68 @@ __device__ __forceinline__ float warp_maxf(float v) {
   return v;
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic (an FP32 pair hi + lo, ~48 significant bits) for
+// the mixture sums of the equation of state, on the FP32 and integer pipes.
+// ---------------------------------------------------------------------------
+struct f2x {
+  float h, l;
+};
+// x = h + l: h is x with its mantissa cut to 24 bits (exact in FP32), l the
+// remainder (29 bits scaled by 2^(e-52)) rounded to FP32.  Values outside
+// the FP32 normal range give h = d2f(x), l = 0.
+__device__ __forceinline__ f2x split64(double x) {
+  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+  const unsigned int ex = (hi >> 20) & 0x7FFu;
+  f2x r;
+  r.h = d2f(__hiloint2double((int)hi, (int)(lo & 0xE0000000u)));  // no rounding: bit 28 is 0
+  const int se = (int)ex - 948;  // biased FP32 exponent of 2^(e - 52)
+  const float scale = (se > 0 && ex - 897u <= 253u) ? __int_as_float(se << 23) : 0.f;
+  r.l = __uint_as_float(__float_as_uint(__uint2float_rn(lo & 0x1FFFFFFFu) * scale) |
+                        (hi & 0x80000000u));
+  return r;
+}
+// s += a * (ch + cl), a given as a split pair: exact product of the high
+// parts (fma residual), first-order cross terms, error-free sum into s.h
+__device__ __forceinline__ void fx_acc(f2x& s, const f2x a, float ch, float cl) {
+  const float p = a.h * ch;
+  float e = fmaf(a.h, ch, -p);
+  e = fmaf(a.h, cl, e);
+  e = fmaf(a.l, ch, e);
+  const float t = s.h + p, bb = t - s.h;
+  s.l += ((s.h - (t - bb)) + (p - bb)) + e;
+  s.h = t;
+}
+// a / b in double-float, returned as hi + lo of ~46 bits
+__device__ __forceinline__ f2x fx_div(const f2x a, const f2x b) {
+  const float r = 1.0f / b.h;
+  const float q1 = a.h * r;
+  const float p = q1 * b.h, pe = fmaf(q1, b.h, -p);
+  const float rem = ((a.h - p) - pe) + (a.l - q1 * b.l);
+  f2x q;
+  q.h = q1;
+  q.l = rem * r;
+  return q;
+}
+
 // One cell of the primitive pass: state index from g, primitive index from
 // gq (the primitive arrays' geometry; equal to g in 2D).  lS / lC
 // accumulate the interior maxima of the wave speed and |C_hat| when `red`
 // is set (reduced by the caller).  mu (3D viscous) receives the mixture
 // viscosity sum_s Y_s mu_s.
 //
-// FP64 work is kept to what the pressure needs: the mixture heat capacities
-// (gamma - 1 = sum rho_s R_s / sum rho_s cv_s) and p = (gamma-1)(E - KE).
+// FP64 instructions are kept to the pressure itself, p = (gamma-1)(E - KE),
+// and E + p.  gamma - 1 = sum rho_s R_s / sum rho_s cv_s is formed in
+// double-float (~1e-14 relative, as the FP64 sums it replaces would need).
 // The kinetic energy is formed in FP32: its error (1e-7 KE) is below the
 // FP32 flux error wherever KE matters and negligible where it does not (the
 // near-hydrostatic states whose pressure gradient needs FP64 accuracy).
 // The pressure goes out as FP64 (pr) or as an FP32 pair hi + lo (pp[q],
 // pp[q + qv]) that carries ~48 bits: differences of neighbouring pressures
 // then come out of FP32 arithmetic (hi - hi' is exact for close values).
-template <int NDIM>
+// NS > 0: the species count at compile time (loops unrolled, every load
+// issued up front); NS = 0: P.ns at run time.
+template <int NDIM, int NS = 0>
 __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Phys& P,
                                            const double* __restrict__ U, float* __restrict__ Q,
                                            float* __restrict__ rho, double* __restrict__ rho64,
@@ -83,19 +135,27 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
   const long long q = (long long)i + gq.sy * j + gq.sz * k;
   const int s0 = NDIM + 1;  // first species index
   // mixture EOS (calculateRhoPT, src/secondary.hpp:60-151)
-  double sCv = 0.0, sRm = 0.0, r64 = 0.0;
+  double r64 = 0.0;
+  f2x sCv{0.f, 0.f}, sRm{0.f, 0.f};
   float rf = 0.f;
-  for (int s = 0; s < P.ns; ++s) {
+  const int ns = NS > 0 ? NS : P.ns;
+#pragma unroll
+  for (int s = 0; s < (NS > 0 ? NS : FST_MAX_SPECIES); ++s) {
+    if (NS == 0 && s >= ns) break;
     const double rs = U[c + sv * (s0 + s)];
     if (rho64) r64 += rs;
-    sCv = fma(rs, P.cv_s[s], sCv);
-    sRm = fma(rs, P.rm_s[s], sRm);
-    rf += d2f(rs);
+    const f2x a = split64(rs);
+    fx_acc(sCv, a, P.cv_f[s], P.cvl_f[s]);
+    fx_acc(sRm, a, P.rm_f[s], P.rml_f[s]);
+    rf += a.h + a.l;
   }
   const float rif = __frcp_rn(rf);
-  const double gm1 = sRm * rcp64(sCv);
+  const f2x g1 = fx_div(sRm, sCv);
+  const double gm1 = f2d(g1.h) + f2d(g1.l);
   float Cv2 = 0.f, Cp2 = 0.f, m = 0.f;
-  for (int s = 0; s < P.ns; ++s) {
+#pragma unroll
+  for (int s = 0; s < (NS > 0 ? NS : FST_MAX_SPECIES); ++s) {
+    if (NS == 0 && s >= ns) break;
     const float rs = d2f(U[c + sv * (s0 + s)]);
     const float ys = rs * rif;
     if (NDIM == 2) {
@@ -127,7 +187,7 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
   Q[q + qv * NDIM] = d2f(E + p);
   rho[q] = rf;
   if (rho64) rho64[q] = r64;
-  if (T) T[q] = d2f(p) / d2f(sRm);  // p / (rho R_mix), R_mix = sum rho_s R_s / rho
+  if (T) T[q] = d2f(p) / (sRm.h + sRm.l);  // p / (rho R_mix), R_mix = sum rho_s R_s / rho
   if (nrg) nrg[q] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
   if (Cc)
     for (int n = 0; n < 5; ++n) Cc[q + qv * n] = d2f(U[c + sv * (P.nv + n)]);
@@ -137,7 +197,7 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
     if (in) {
       const float pf = d2f(p), mf = sqrtf(msq);
       float sp;
-      if (NDIM == 3) sp = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
+      if (NDIM == 3) sp = sqrtf((1.0f + g1.h) * pf * rif) + mf * rif;
       else sp = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
       lS = fmaxf(lS, sp);
       lC = fmaxf(lC, fabsf(Cc[q + qv]));

@@ -829,6 +829,11 @@ class Deck:
     periodic: tuple = (False, False, False)
     bcs: tuple = (0, 0, 0, 0, 0, 0)
     noise: bool = False
+    noise_dh: float = 0.0
+    noise_eta: float = 0.0
+    noise_coff: float = 0.0
+    noise_nt: int = 1
+    noise_mode: int = 1
     scheme: str = "weno5"
     grid: str = "cartesian"
     ng: int = 3
@@ -847,6 +852,13 @@ class Deck:
                                bcs=self.bcs, mode=self.mode, audit_every=self.audit_every,
                                dx=list(self.dx) + [self.dx[0]] * (3 - len(self.dx)),
                                classify_every=self.classify_every)
+
+    def noise_params(self):
+        """abi.FstNoiseParams of fiesta.noise, or None when the filter is off."""
+        if not self.noise:
+            return None
+        return abi.FstNoiseParams(dh=self.noise_dh, eta=self.noise_eta, coff=self.noise_coff,
+                                  nt=self.noise_nt, mode=self.noise_mode)
 
     def initial_conditions(self, cfg=None):
         """Evaluate ``fiesta.initial_conditions(x, y, z, v)`` at every interior
@@ -995,6 +1007,12 @@ def load(path=None, text=None):
         d.beta = rd.get(["ceq", "beta"], float)
         d.betae = rd.get(["ceq", "betae"], float)
     d.noise = rd.get(["noise", "enabled"], bool, False)
+    if d.noise:  # src/input.cpp:270-277
+        d.noise_dh = rd.get(["noise", "dh"], float)
+        d.noise_eta = rd.get(["noise", "eta"], float)
+        d.noise_coff = rd.get(["noise", "coff"], float)
+        d.noise_nt = rd.get(["noise", "nt"], int, 1)
+        d.noise_mode = rd.get(["noise", "mode"], int, 1)
     zper = False
     if d.ndim == 3:
         zper = rd.get(["bc", "zperiodic"], bool, False)

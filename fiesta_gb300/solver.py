@@ -44,6 +44,7 @@ _EXPORTS = {
     "fst_rk_step": (C.c_int, [C.c_void_p, C.c_int]),
     "fst_secondary": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_check_finite": (C.c_int, [C.c_void_p]),
+    "fst_noise_filter": (C.c_int, [C.c_void_p, C.POINTER(abi.FstNoiseParams)]),
     "fst_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                              C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fst_get_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.FstStats)]),
@@ -186,6 +187,11 @@ class Solver:
                                      _dptr(xmin) if secondary else nul,
                                      _dptr(xmax) if secondary else nul), "status")
         return vmin, vmax, xmin, xmax
+
+    def noise_filter(self, dh, eta, coff=0.0, nt=1, mode=1):
+        """The postStep noise filter (fiesta.noise.*) on the current state."""
+        np_ = abi.FstNoiseParams(dh=dh, eta=eta, coff=coff, nt=nt, mode=mode)
+        self._check(lib().fst_noise_filter(self._ctx, C.byref(np_)), "noise_filter")
 
     def check_finite(self):
         rc = lib().fst_check_finite(self._ctx)

@@ -182,6 +182,28 @@ int fst_status(fst_ctx* ctx, double* vmin, double* vmax, double* xmin, double* x
 
 int fst_get_stats(const fst_ctx* ctx, fst_stats* out);
 
+/* Noise filter parameters: fiesta.noise.{dh, eta, coff, nt, mode}
+ * (src/input.cpp:270-277). */
+typedef struct fst_noise_params {
+  double dh;                 /* detection threshold factor                   */
+  double eta;                /* diffusion coefficient of the removal sweep   */
+  double coff;               /* C_hat cutoff factor (used when ceq is on)    */
+  int nt;                    /* removal sweeps per variable                  */
+  int mode;                  /* 1: momenta; otherwise the energy             */
+  int reserved[6];
+} fst_noise_params;
+
+/* The postStep noise filter of the current state (src/cart3d.cpp:319-374,
+ * src/cart2d.cpp:257-307; detectNoise / removeNoise, src/noise.hpp:26-262):
+ * per filtered variable, detection on a lattice of 3x3(x3) blocks, then `nt`
+ * in-place diffusion sweeps over the flagged cells.  The reference's removal
+ * updates the state in place while neighbours read it, so its result is that
+ * of a sweep in loop order (i slowest); this entry point reproduces that
+ * order exactly (tile wavefronts), giving the reference's serial result bit
+ * for bit.  The noise indicator persists between calls, as the module's
+ * member array does. */
+int fst_noise_filter(fst_ctx* ctx, const fst_noise_params* np);
+
 /* Per-kernel device timing (the reference's per-region fiestaTimer,
  * src/timer.hpp:52-119, reset/accumulated around kernels in
  * src/cart3d.cpp:201-218).  With profiling on, every kernel launch is

@@ -873,6 +873,119 @@ struct Oracle {
   }
 
   // secondary variables of the current state (postStep path)
+  // ---- noise filter: postStep (src/cart3d.cpp:319-374, src/cart2d.cpp:257-307)
+  // with detectNoise3D/removeNoise3D and the 2D pair (src/noise.hpp:26-262).
+  // Serial, in the MDRange loop order (first index slowest): the removal
+  // updates var in place while neighbours read it.
+  std::vector<int> noise;  // FS3D_I / FS2D_I, zero-initialised, kept between calls
+  inline int& NZ(int i, int j, int k) { return noise[c3(i, j, k)]; }
+
+  void noise_filter(double n_dh, double n_eta, double n_coff, int n_nt, int n_mode) {
+    if (noise.empty()) noise.assign((size_t)ngi * ngj * ngk, 0);
+    const int M = (nci + 1) % 2 == 0 ? (nci + 1) / 2 : nci / 2;
+    const int N = (ncj + 1) % 2 == 0 ? (ncj + 1) / 2 : ncj / 2;
+    const int L = (nck + 1) % 2 == 0 ? (nck + 1) / 2 : nck / 2;
+    double coff = 0.0;
+    if (cf.ceq) {
+      // 3D: maxCvar3D(var, 6), a fixed variable index; 2D: maxCvar2D(var, 1, cd)
+      // = |var(nv+1)|.  Serial max from -DBL_MAX with `s > lmax`.
+      const int cv = ndim == 3 ? 6 : nv + 1;
+      double mx = -DBL_MAX;
+      for (int i = ng; i < ngi - ng; ++i)
+        for (int j = ng; j < ngj - ng; ++j)
+          for (int k = (ndim == 3 ? ng : 0); k < (ndim == 3 ? ngk - ng : 1); ++k) {
+            double s = std::fabs(V(i, j, k, cv));
+            if (s > mx) mx = s;
+          }
+      coff = n_coff * mx;
+    }
+    std::vector<int> vars;
+    if (n_mode == 1) {
+      for (int d = 0; d < ndim; ++d) vars.push_back(d);
+    } else {
+      vars.push_back(ndim);
+    }
+    for (int v : vars) {
+      if (ndim == 3) {
+        for (int ii = 0; ii < M + 1; ++ii)
+          for (int jj = 0; jj < N + 1; ++jj)
+            for (int kk = 0; kk < L + 1; ++kk) detect3(ii, jj, kk, v, n_dh, coff);
+        for (int tau = 0; tau < n_nt; ++tau)
+          for (int i = ng; i < ngi - ng; ++i)
+            for (int j = ng; j < ngj - ng; ++j)
+              for (int k = ng; k < ngk - ng; ++k) {
+                const double lap = (V(i - 1, j, k, v) - 2 * V(i, j, k, v) + V(i + 1, j, k, v)) / (dx * dx) +
+                                   (V(i, j - 1, k, v) - 2 * V(i, j, k, v) + V(i, j + 1, k, v)) / (dy * dy) +
+                                   (V(i, j, k - 1, v) - 2 * V(i, j, k, v) + V(i, j, k + 1, v)) / (dz * dz);
+                const double dnoise = n_eta * (dx * dx + dy * dy + dz * dz) * NZ(i, j, k) * lap;
+                V(i, j, k, v) += dnoise;
+              }
+      } else {
+        for (int ii = 0; ii < M + 1; ++ii)
+          for (int jj = 0; jj < N + 1; ++jj) detect2(ii, jj, v, n_dh, coff);
+        for (int tau = 0; tau < n_nt; ++tau)
+          for (int i = ng; i < ngi - ng; ++i)
+            for (int j = ng; j < ngj - ng; ++j) {
+              const double lgrad = (V(i, j, 0, v) - V(i - 1, j, 0, v)) / dx;
+              const double rgrad = (V(i + 1, j, 0, v) - V(i, j, 0, v)) / dx;
+              const double bgrad = (V(i, j, 0, v) - V(i, j - 1, 0, v)) / dy;
+              const double tgrad = (V(i, j + 1, 0, v) - V(i, j, 0, v)) / dy;
+              const double dv = n_eta * (dx * dx + dy * dy) * NZ(i, j, 0) *
+                                ((rgrad - lgrad) / dx + (tgrad - bgrad) / dy);
+              V(i, j, 0, v) += dv;
+            }
+      }
+    }
+  }
+  // detectNoise3D at lattice point (ii, jj, kk)
+  void detect3(int ii, int jj, int kk, int v, double dh, double coff) {
+    const int i = 2 * ii + ng, j = 2 * jj + ng, k = 2 * kk + ng;
+    const double a = std::sqrt(165.0 * dx * dy * dz) / 15840.0;
+    // the 27 weights in the reference's term order: planes k+1, k, k-1;
+    // rows j+1, j, j-1; columns i-1, i, i+1
+    static const double w[3][3][3] = {{{2, 2, 2}, {2, 8, 2}, {2, 2, 2}},
+                                      {{2, 8, 2}, {8, -88, 8}, {2, 8, 2}},
+                                      {{2, 2, 2}, {2, 8, 2}, {2, 2, 2}}};
+    double sum = 0.0;
+    bool first = true;
+    for (int pk = 0; pk < 3; ++pk)
+      for (int rj = 0; rj < 3; ++rj)
+        for (int ci = 0; ci < 3; ++ci) {
+          const double t = w[pk][rj][ci] * V(i - 1 + ci, j + 1 - rj, k + 1 - pk, v);
+          sum = first ? t : sum + t;
+          first = false;
+        }
+    const double c = -a * sum;
+    const double cref = dh * std::sqrt(dx * dy * dz / 12.0);
+    for (int a1 = -1; a1 < 2; ++a1)
+      for (int b1 = -1; b1 < 2; ++b1)
+        for (int c1 = -1; c1 < 2; ++c1) NZ(i + a1, j + b1, k + c1) = 0;
+    if (std::fabs(c) >= cref) {
+      for (int a1 = -1; a1 < 2; ++a1)
+        for (int b1 = -1; b1 < 2; ++b1)
+          for (int c1 = -1; c1 < 2; ++c1)
+            if (coff == 0.0 || std::fabs(V(i + a1, j + b1, k + c1, nv + 1)) < coff)
+              NZ(i + a1, j + b1, k + c1) = 1;
+    }
+  }
+  // detectNoise2D at lattice point (ii, jj): no abs() on the C_hat test
+  void detect2(int ii, int jj, int v, double dh, double coff) {
+    const int i = 2 * ii + ng, j = 2 * jj + ng;
+    const double a = std::sqrt(6.0 * dx * dy);
+    const double c = -(a / 192.0) *
+                     (V(i - 1, j + 1, 0, v) + 2 * V(i, j + 1, 0, v) + V(i + 1, j + 1, 0, v) +
+                      2 * V(i - 1, j, 0, v) - 12 * V(i, j, 0, v) + 2 * V(i + 1, j, 0, v) +
+                      V(i - 1, j - 1, 0, v) + 2 * V(i, j - 1, 0, v) + V(i + 1, j - 1, 0, v));
+    const double cref = dh * a / 16.0;
+    for (int a1 = -1; a1 < 2; ++a1)
+      for (int b1 = -1; b1 < 2; ++b1) NZ(i + a1, j + b1, 0) = 0;
+    if (std::fabs(c) >= cref) {
+      for (int a1 = -1; a1 < 2; ++a1)
+        for (int b1 = -1; b1 < 2; ++b1)
+          if (coff == 0.0 || V(i + a1, j + b1, 0, nv + 1) < coff) NZ(i + a1, j + b1, 0) = 1;
+    }
+  }
+
   void secondary(double* out, size_t n) {
     const size_t nc = (size_t)ngi * ngj * ngk;
     const int nf = ndim == 3 ? 6 : 5;
@@ -967,6 +1080,21 @@ int orc_secondary(orc_ctx* c, double* out, size_t n) {
 int orc_last_max(const orc_ctx* c, double* maxS, double* maxCh) {
   *maxS = c->o.last_maxS;
   *maxCh = c->o.last_maxCh;
+  return FST_OK;
+}
+int orc_noise_filter(orc_ctx* c, const fst_noise_params* np) {
+  if (!np) return FST_ERR_INVALID;
+  c->o.noise_filter(np->dh, np->eta, np->coff, np->nt, np->mode);
+  return FST_OK;
+}
+int orc_get_noise(orc_ctx* c, int* out, size_t n) {
+  Oracle& o = c->o;
+  if (n != (size_t)o.ngi * o.ngj * o.ngk) return FST_ERR_SIZE;
+  for (int k = 0; k < o.ngk; ++k)
+    for (int j = 0; j < o.ngj; ++j)
+      for (int i = 0; i < o.ngi; ++i)
+        out[(size_t)i + (size_t)o.ngi * (j + (size_t)o.ngj * k)] =
+            o.noise.empty() ? 0 : o.noise[o.c3(i, j, k)];
   return FST_OK;
 }
 int orc_set_threads(int n) {

@@ -106,6 +106,17 @@ class _Checker:
     def rk_step(self, nsteps=1):
         self._call("rk_step", C.c_int(nsteps))
 
+    def noise_filter(self, dh, eta, coff=0.0, nt=1, mode=1):
+        """The postStep noise filter (serial loop order)."""
+        from fiesta_gb300 import abi
+        np_ = abi.FstNoiseParams(dh=dh, eta=eta, coff=coff, nt=nt, mode=mode)
+        self._call("noise_filter", C.byref(np_))
+
+    def noise(self):
+        out = np.zeros(self.shape[:3], dtype=np.int32, order="F")
+        self._call("get_noise", out.ctypes.data_as(C.POINTER(C.c_int)), C.c_size_t(out.size))
+        return out
+
     def secondary(self):
         nf = 6 if self.cfg.ndim == 3 else 5
         shp = self.shape[:3] + (nf,)

@@ -7,6 +7,8 @@
 //
 // The time loop mirrors src/main.cpp:61-72 / Fiesta::step
 // (src/fiesta.cpp:333-340): preStep, rkAdvance, postStep, t += 1.
+#include <omp.h>
+
 #include <cstring>
 #include <memory>
 
@@ -144,6 +146,51 @@ int ref_secondary(ref_ctx* x, double* out, size_t n) {
   size_t nf = x->cf.ndim == 3 ? 6 : 5;
   if (n != nc * nf) return FST_ERR_SIZE;
   std::memcpy(out, vx.data(), n * sizeof(double));
+  return 0;
+}
+
+// postStep with the noise filter on (src/cart3d.cpp:300-374,
+// src/cart2d.cpp:239-307), its kernels run on one thread: the removal
+// updates var in place while neighbours read it, so only the serial loop
+// order gives a defined result.
+int ref_noise_filter(ref_ctx* x, const fst_noise_params* np) {
+  inputConfig& cf = x->cf;
+  cf.noise = true;
+  cf.n_dh = np->dh;
+  cf.n_eta = np->eta;
+  cf.n_coff = np->coff;
+  cf.n_nt = np->nt;
+  cf.n_mode = np->mode;
+  if (cf.ndim == 3) {
+    auto* f = dynamic_cast<cart3d_func*>(x->f.get());
+    if (f->noise.size() == 0) f->noise = FS3D_I("noise", cf.ngi, cf.ngj, cf.ngk);
+  } else {
+    auto* f = dynamic_cast<cart2d_func*>(x->f.get());
+    if (f->noise.size() == 0) f->noise = FS2D_I("noise", cf.ngi, cf.ngj);
+  }
+  const int nth = omp_get_max_threads();
+  omp_set_num_threads(1);
+  x->f->postStep();
+  omp_set_num_threads(nth);
+  cf.noise = false;
+  return 0;
+}
+int ref_get_noise(ref_ctx* x, int* out, size_t n) {
+  const inputConfig& cf = x->cf;
+  if (n != (size_t)cf.ngi * cf.ngj * cf.ngk) return FST_ERR_SIZE;
+  for (int k = 0; k < cf.ngk; ++k)
+    for (int j = 0; j < cf.ngj; ++j)
+      for (int i = 0; i < cf.ngi; ++i) {
+        int v = 0;
+        if (cf.ndim == 3) {
+          auto* f = dynamic_cast<cart3d_func*>(x->f.get());
+          if (f->noise.size()) v = f->noise(i, j, k);
+        } else {
+          auto* f = dynamic_cast<cart2d_func*>(x->f.get());
+          if (f->noise.size()) v = f->noise(i, j);
+        }
+        out[(size_t)i + (size_t)cf.ngi * (j + (size_t)cf.ngj * k)] = v;
+      }
   return 0;
 }
 

@@ -64,6 +64,11 @@ def test_deck_keys_and_config():
     assert d.periodic == (True, False, False)
     assert d.bcs == (0, 0, abi.BC_NOSLIP, abi.BC_REFLECTIVE, abi.BC_HYDROSTATIC, abi.BC_OUTFLOW)
     assert d.mode == abi.MODE_MIXED
+    assert d.noise_params() is None
+    dn = deck.load(text=DECK_3D + "\nfiesta.noise.enabled=true\nfiesta.noise.dh=1e-5\n"
+                   "fiesta.noise.eta=1e-3\nfiesta.noise.coff=0.05\n")
+    np_ = dn.noise_params()
+    assert (np_.dh, np_.eta, np_.coff, np_.nt, np_.mode) == (1e-5, 1e-3, 0.05, 1, 1)
     cfg = d.config()
     assert (cfg.nci, cfg.ncj, cfg.nck, cfg.ns) == (32, 16, 8, 2)
     assert cfg.dz == 0.25 / 8 and cfg.g_accel == 9.81 and cfg.xper == 1

@@ -1,0 +1,63 @@
+"""The postStep noise filter (src/cart3d.cpp:319-374, src/cart2d.cpp:257-307,
+src/noise.hpp): the oracle against the reference's own sources compiled here
+(serial loop order, the only order with a defined result), and the library's
+fst_noise_filter against the oracle, bit for bit."""
+import numpy as np
+import pytest
+
+from fiesta_gb300 import abi
+from fiesta_gb300.solver import initial_conditions
+from oracle.oracle import Oracle, Reference
+from tests.golden_io import same
+
+CASES = [  # ndim, cells, ceq, mode, nt, dh, coff
+    (3, (9, 8, 7), False, 1, 1, 1e-3, 0.0),
+    (3, (10, 7, 6), True, 1, 2, 1e-3, 0.5),
+    (3, (8, 8, 8), True, 2, 1, 1e-2, 0.0),
+    (3, (19, 17, 10), True, 1, 1, 5e-4, 0.8),
+    (2, (20, 17), False, 1, 1, 1e-3, 0.0),
+    (2, (19, 22), True, 2, 2, 1e-4, 0.3),
+    (2, (37, 33), True, 1, 1, 1e-3, 0.2),
+]
+
+
+def _case(ndim, n, ceq, seed):
+    sp = [dict(gamma=1.4, M=1.0, mu=1e-3)]
+    cfg = abi.make_config(ndim, n, dt=1e-4, species=sp, R=1.0, ceq=ceq)
+    rng = np.random.default_rng(seed)
+    U = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, seed)
+    U = np.asfortranarray(U * (1 + 0.05 * rng.standard_normal(U.shape)))  # roughness
+    if ceq:
+        U[..., abi.nv_of(cfg) + 1] = np.abs(rng.standard_normal(U.shape[:3]))
+    return cfg, U
+
+
+@pytest.mark.skipif(not Reference.available(), reason="reference checker not built")
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_noise_matches_reference(case):
+    ndim, n, ceq, mode, nt, dh, coff = case
+    cfg, U = _case(ndim, n, ceq, 4)
+    o, r = Oracle(cfg), Reference(cfg)
+    o.set_state(U)
+    r.set_state(U)
+    for _ in range(2):  # the indicator persists between calls
+        o.noise_filter(dh, 0.1, coff, nt, mode)
+        r.noise_filter(dh, 0.1, coff, nt, mode)
+        assert same(o.get_state(), r.get_state())
+        assert np.array_equal(o.noise(), r.noise())
+    assert int(o.noise().sum()) > 0 and not np.array_equal(o.get_state(), U)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_gpu_noise_matches_oracle(case):
+    from fiesta_gb300.solver import Solver
+    ndim, n, ceq, mode, nt, dh, coff = case
+    cfg, U = _case(ndim, n, ceq, 5)
+    o, s = Oracle(cfg), Solver(cfg)
+    o.set_state(U)
+    s.set_state(U)
+    for _ in range(2):
+        o.noise_filter(dh, 0.1, coff, nt, mode)
+        s.noise_filter(dh, 0.1, coff, nt, mode)
+        assert same(s.get_state(), o.get_state())
