@@ -500,7 +500,14 @@ def main():
                    "within rel-L2 1e-5 of the FP64 path after warmup+steps steps",
                    "dt": dt, "l2": "state 2.0 GB > L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": r["roofline"], "cpu_baseline": cpu, "clocks": r["clocks"],
+        "roofline": r["roofline"],
+        # whole-step figure: the compulsory FP64 state traffic of a fused
+        # two-stage RK step, 5 * nvt * 8 bytes per interior cell-step
+        "roofline_step": {"bytes_per_cell_step": 5 * 14 * 8,
+                          "achieved": value * 1e6 * 5 * 14 * 8 / 1e9, "unit": "GB/s",
+                          "peak": peak, "frac": value * 1e6 * 5 * 14 * 8 / 1e9 / peak,
+                          "peak_source": peak_kind},
+        "cpu_baseline": cpu, "clocks": r["clocks"],
         "e2e": r["e2e"], "gpu_launches": r["gpu_launches"],
         "modes": {m: {k: v for k, v in results[m].items() if k not in ("clocks",)} for m in modes},
         "batch2d": batch,

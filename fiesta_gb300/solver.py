@@ -73,6 +73,8 @@ def lib():
             raise RuntimeError(f"libfst.so not found at {path}; run __graft_entry__.build()")
         L = C.CDLL(path)
         for name, (res, args) in _EXPORTS.items():
+            if os.environ.get("FST_LIB") and not hasattr(L, name):
+                continue  # an older build of the library: bind what it has
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
