@@ -179,8 +179,6 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
     P.rm_s[s] = P.cp_s[s] - P.cv_s[s];
     P.cv_f[s] = (float)P.cv_s[s];
     P.rm_f[s] = (float)(P.cp_s[s] - P.cv_s[s]);
-    P.cvl_f[s] = (float)(P.cv_s[s] - (double)P.cv_f[s]);
-    P.rml_f[s] = (float)(P.rm_s[s] - (double)P.rm_f[s]);
     P.mu_f[s] = (float)P.mu_s[s];
     P.cv2_f[s] = (float)P.cv2_s[s];
     P.cp2_f[s] = (float)P.cp2_s[s];

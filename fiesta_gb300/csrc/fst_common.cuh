@@ -54,8 +54,6 @@ struct Phys {
   // FP32 copies for the mixed path: cv_s, R_s = cp_s - cv_s, mu_s, and the
   // stride-2 table constants
   float cv_f[FST_MAX_SPECIES], rm_f[FST_MAX_SPECIES], mu_f[FST_MAX_SPECIES];
-  // the FP32 remainders cv_s - cv_f, R_s - rm_f (double-float constants)
-  float cvl_f[FST_MAX_SPECIES], rml_f[FST_MAX_SPECIES];
   float cv2_f[FST_MAX_SPECIES], cp2_f[FST_MAX_SPECIES];
   // FP32 copies of the grid constants (mixed path)
   float rd_f[3];    // 1/dx, 1/dy, 1/dz

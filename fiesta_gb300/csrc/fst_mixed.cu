@@ -29,7 +29,7 @@
 namespace {
 using namespace fstm;
 
-template <int NDIM, int NS>
+template <int NDIM>
 __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const double* __restrict__ U,
                                                float* __restrict__ Q, float* __restrict__ rho,
                                                double* __restrict__ rho64,
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const doub
   const int j = t / g.ngi, i = t - j * g.ngi;
   float lS = -3.0e38f, lC = -3.0e38f;
   if (j < g.ngj)
-    mprim_cell<NDIM, NS>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red != nullptr, i, j,
+    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red != nullptr, i, j,
                      blockIdx.z, lS, lC);
   if (red) {
     lS = warp_maxf(lS);
@@ -86,23 +86,13 @@ __global__ void __launch_bounds__(64) k_mghost(Geo g, const double* __restrict__
 
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 
-// k_mprim for the run's species count (unrolled up to five species)
+// k_mprim over all cells in storage order
 template <int NDIM>
 void launch_mprim(const Geo& g, const Geo& gq, const Phys& P, const double* U, float* Q,
                   float* rho, double* rho64, float* vel, double* pr, float* pp, float* mu,
                   float* nrg, float* Cc, float* T, unsigned long long* red, cudaStream_t st) {
   const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
-#define FST_MPRIM(NSV) \
-  k_mprim<NDIM, NSV><<<qg, qb, 0, st>>>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red)
-  switch (g.ns) {
-    case 1: FST_MPRIM(1); break;
-    case 2: FST_MPRIM(2); break;
-    case 3: FST_MPRIM(3); break;
-    case 4: FST_MPRIM(4); break;
-    case 5: FST_MPRIM(5); break;
-    default: FST_MPRIM(0); break;
-  }
-#undef FST_MPRIM
+  k_mprim<NDIM><<<qg, qb, 0, st>>>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red);
 }
 
 // Launch the fused 2D RHS for a compile-time variable count.

@@ -60,68 +60,21 @@ __device__ __forceinline__ float warp_maxf(float v) {
   return v;
 }
 
-// ---------------------------------------------------------------------------
-// Double-float arithmetic (an FP32 pair hi + lo, ~48 significant bits) for
-// the mixture sums of the equation of state, on the FP32 and integer pipes.
-// ---------------------------------------------------------------------------
-struct f2x {
-  float h, l;
-};
-// x = h + l: h is x with its mantissa cut to 24 bits (exact in FP32), l the
-// remainder (29 bits scaled by 2^(e-52)) rounded to FP32.  Values outside
-// the FP32 normal range give h = d2f(x), l = 0.
-__device__ __forceinline__ f2x split64(double x) {
-  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
-  const unsigned int ex = (hi >> 20) & 0x7FFu;
-  f2x r;
-  r.h = d2f(__hiloint2double((int)hi, (int)(lo & 0xE0000000u)));  // no rounding: bit 28 is 0
-  const int se = (int)ex - 948;  // biased FP32 exponent of 2^(e - 52)
-  const float scale = (se > 0 && ex - 897u <= 253u) ? __int_as_float(se << 23) : 0.f;
-  r.l = __uint_as_float(__float_as_uint(__uint2float_rn(lo & 0x1FFFFFFFu) * scale) |
-                        (hi & 0x80000000u));
-  return r;
-}
-// s += a * (ch + cl), a given as a split pair: exact product of the high
-// parts (fma residual), first-order cross terms, error-free sum into s.h
-__device__ __forceinline__ void fx_acc(f2x& s, const f2x a, float ch, float cl) {
-  const float p = a.h * ch;
-  float e = fmaf(a.h, ch, -p);
-  e = fmaf(a.h, cl, e);
-  e = fmaf(a.l, ch, e);
-  const float t = s.h + p, bb = t - s.h;
-  s.l += ((s.h - (t - bb)) + (p - bb)) + e;
-  s.h = t;
-}
-// a / b in double-float, returned as hi + lo of ~46 bits
-__device__ __forceinline__ f2x fx_div(const f2x a, const f2x b) {
-  const float r = 1.0f / b.h;
-  const float q1 = a.h * r;
-  const float p = q1 * b.h, pe = fmaf(q1, b.h, -p);
-  const float rem = ((a.h - p) - pe) + (a.l - q1 * b.l);
-  f2x q;
-  q.h = q1;
-  q.l = rem * r;
-  return q;
-}
-
 // One cell of the primitive pass: state index from g, primitive index from
 // gq (the primitive arrays' geometry; equal to g in 2D).  lS / lC
 // accumulate the interior maxima of the wave speed and |C_hat| when `red`
 // is set (reduced by the caller).  mu (3D viscous) receives the mixture
 // viscosity sum_s Y_s mu_s.
 //
-// FP64 instructions are kept to the pressure itself, p = (gamma-1)(E - KE),
-// and E + p.  gamma - 1 = sum rho_s R_s / sum rho_s cv_s is formed in
-// double-float (~1e-14 relative, as the FP64 sums it replaces would need).
+// FP64 work is kept to what the pressure needs: the mixture heat capacities
+// (gamma - 1 = sum rho_s R_s / sum rho_s cv_s) and p = (gamma-1)(E - KE).
 // The kinetic energy is formed in FP32: its error (1e-7 KE) is below the
 // FP32 flux error wherever KE matters and negligible where it does not (the
 // near-hydrostatic states whose pressure gradient needs FP64 accuracy).
 // The pressure goes out as FP64 (pr) or as an FP32 pair hi + lo (pp[q],
 // pp[q + qv]) that carries ~48 bits: differences of neighbouring pressures
 // then come out of FP32 arithmetic (hi - hi' is exact for close values).
-// NS > 0: the species count at compile time (loops unrolled, every load
-// issued up front); NS = 0: P.ns at run time.
-template <int NDIM, int NS = 0>
+template <int NDIM>
 __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Phys& P,
                                            const double* __restrict__ U, float* __restrict__ Q,
                                            float* __restrict__ rho, double* __restrict__ rho64,
@@ -135,27 +88,22 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
   const long long q = (long long)i + gq.sy * j + gq.sz * k;
   const int s0 = NDIM + 1;  // first species index
   // mixture EOS (calculateRhoPT, src/secondary.hpp:60-151)
-  double r64 = 0.0;
-  f2x sCv{0.f, 0.f}, sRm{0.f, 0.f};
+  // The species loop stays rolled: unrolling it (all loads issued up front)
+  // measured 1.5x slower for this streaming pass on GB300, as did forming
+  // the two sums in double-float on the FP32 pipe.
+  double sCv = 0.0, sRm = 0.0, r64 = 0.0;
   float rf = 0.f;
-  const int ns = NS > 0 ? NS : P.ns;
-#pragma unroll
-  for (int s = 0; s < (NS > 0 ? NS : FST_MAX_SPECIES); ++s) {
-    if (NS == 0 && s >= ns) break;
+  for (int s = 0; s < P.ns; ++s) {
     const double rs = U[c + sv * (s0 + s)];
     if (rho64) r64 += rs;
-    const f2x a = split64(rs);
-    fx_acc(sCv, a, P.cv_f[s], P.cvl_f[s]);
-    fx_acc(sRm, a, P.rm_f[s], P.rml_f[s]);
-    rf += a.h + a.l;
+    sCv = fma(rs, P.cv_s[s], sCv);
+    sRm = fma(rs, P.rm_s[s], sRm);
+    rf += d2f(rs);
   }
   const float rif = __frcp_rn(rf);
-  const f2x g1 = fx_div(sRm, sCv);
-  const double gm1 = f2d(g1.h) + f2d(g1.l);
+  const double gm1 = sRm * rcp64(sCv);
   float Cv2 = 0.f, Cp2 = 0.f, m = 0.f;
-#pragma unroll
-  for (int s = 0; s < (NS > 0 ? NS : FST_MAX_SPECIES); ++s) {
-    if (NS == 0 && s >= ns) break;
+  for (int s = 0; s < P.ns; ++s) {
     const float rs = d2f(U[c + sv * (s0 + s)]);
     const float ys = rs * rif;
     if (NDIM == 2) {
@@ -187,7 +135,7 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
   Q[q + qv * NDIM] = d2f(E + p);
   rho[q] = rf;
   if (rho64) rho64[q] = r64;
-  if (T) T[q] = d2f(p) / (sRm.h + sRm.l);  // p / (rho R_mix), R_mix = sum rho_s R_s / rho
+  if (T) T[q] = d2f(p) / d2f(sRm);  // p / (rho R_mix), R_mix = sum rho_s R_s / rho
   if (nrg) nrg[q] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
   if (Cc)
     for (int n = 0; n < 5; ++n) Cc[q + qv * n] = d2f(U[c + sv * (P.nv + n)]);
@@ -197,7 +145,7 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
     if (in) {
       const float pf = d2f(p), mf = sqrtf(msq);
       float sp;
-      if (NDIM == 3) sp = sqrtf((1.0f + g1.h) * pf * rif) + mf * rif;
+      if (NDIM == 3) sp = sqrtf((1.0f + d2f(gm1)) * pf * rif) + mf * rif;
       else sp = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
       lS = fmaxf(lS, sp);
       lC = fmaxf(lC, fabsf(Cc[q + qv]));
