@@ -224,6 +224,9 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
         s.set_profiling(True)
         s.kernel_times()
         torch.cuda.synchronize()
+        import torch.distributed as dist
+        if dist.is_available() and dist.is_initialized():
+            dist.barrier()  # ranks start the timed region together
         t_start = time.perf_counter()
         ev0.record(stream)
         for _ in range(steps):
@@ -405,6 +408,17 @@ def cpu_sample(n_sample=128, steps=1):
                       f"(CPU oracle, OpenMP, {cores} threads, {dt:.1f} s)"}
 
 
+def replica_value(ms, n, world, device):
+    """Whole-job Mcell-steps/s of `world` replicas of an n^3 case: every rank
+    runs the whole case, the slowest rank's ms per step sets the pace."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    return world * (n ** 3) / (ms / 1e3) / 1e6, ms
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -480,11 +494,7 @@ def main():
     r = results[head]
     value, ms = r["value"], r["ms_per_step"]
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        value = world * (n ** 3) / (ms / 1e3) / 1e6
+        value, ms = replica_value(ms, n, world, "cuda")
     if rank != 0:
         return
     batch = None if a.no_batch else run_batch2d(a.steps, a.warmup)
