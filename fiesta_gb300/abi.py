@@ -30,6 +30,14 @@ MODE_PLAIN_FP64 = 0
 MODE_MIXED = 1
 MODE_HYBRID = 2
 
+GRID_CARTESIAN = 0
+GRID_GENERALIZED = 1
+
+SCHEME_WENO5 = 1
+SCHEME_CENTERED4 = 2
+SCHEME_QUICK = 3
+SCHEME_NAMES = {"weno5": SCHEME_WENO5, "centered4": SCHEME_CENTERED4, "quick": SCHEME_QUICK}
+
 IC_SHOCK_TUBE_2D = 1
 IC_EXPANSION_3D = 2
 IC_MIXING_3D = 3
@@ -62,7 +70,9 @@ class FstConfig(C.Structure):
         ("mode", C.c_int),
         ("audit_every", C.c_int),
         ("classify_every", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("grid_type", C.c_int),
+        ("scheme", C.c_int),
+        ("reserved", C.c_int * 5),
     ]
 
 
@@ -107,7 +117,7 @@ def make_config(ndim=3, n=(8, 8, 8), L=(1.0, 1.0, 1.0), dt=1e-6, species=None,
                 R=8.314462, visc=False, ceq=False, kap=10.0, eps=0.4, alpha=40.0,
                 buoyancy=False, g=9.81, rho_ref=0.0, periodic=(False, False, False),
                 bcs=("outflow",) * 6, mode=MODE_PLAIN_FP64, audit_every=0, dx=None,
-                classify_every=1):
+                classify_every=1, grid_type=GRID_CARTESIAN, scheme=SCHEME_WENO5):
     """Build an FstConfig from deck-like arguments.
 
     ``species`` is a list of dicts {gamma, M, mu} as in ``fiesta.species``.
@@ -143,7 +153,21 @@ def make_config(ndim=3, n=(8, 8, 8), L=(1.0, 1.0, 1.0), dt=1e-6, species=None,
     cfg.mode = mode
     cfg.audit_every = audit_every
     cfg.classify_every = classify_every
+    cfg.grid_type = grid_type
+    cfg.scheme = SCHEME_NAMES[scheme] if isinstance(scheme, str) else int(scheme)
     return cfg
+
+
+def grid_dims(cfg):
+    """(ni, nj, nk, 3) of the node-coordinate array of a generalized grid."""
+    nk = cfg.nck + 1 if cfg.ndim == 3 else 1
+    return cfg.nci + 1, cfg.ncj + 1, nk, 3
+
+
+def metrics_dims(cfg):
+    """(ngi, ngj, ngk, d, d) of the metric tensor array."""
+    ngi, ngj, ngk, _ = dims(cfg)
+    return ngi, ngj, ngk, cfg.ndim, cfg.ndim
 
 
 def dims(cfg):

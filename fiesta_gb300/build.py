@@ -1,7 +1,7 @@
 """In-tree build of libfst.so for sm_103a (nvcc, no cmake).
 
 Translation units and their floating-point contract:
-  fst_plain3d.cu, fst_plain2d.cu, fst_bc.cu, fst_noise.cu
+  fst_plain3d.cu, fst_plain2d.cu, fst_bc.cu, fst_noise.cu, fst_gen.cu
                                               --fmad=false: the plain FP64 path
       reproduces the reference's FP64 arithmetic operation for operation
   fst_mixed.cu, fst_mixed3d.cu, fst_hybrid.cu, fst_batch.cu
@@ -36,6 +36,7 @@ UNITS = [
     ("fst_api.cu", ["--fmad=false"]),
     ("fst_noalloc.cu", ["--fmad=false"]),
     ("fst_noise.cu", ["--fmad=false"]),
+    ("fst_gen.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["fst_host.cpp"]
 

@@ -55,6 +55,8 @@ struct fst_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
   int* dflag = nullptr;
+  bool gen = false;       // FST_GRID_GENERALIZED
+  bool grid_set = false;  // fst_set_grid has computed the metrics
   Prof prof;
 };
 
@@ -101,6 +103,18 @@ std::string validate(const fst_config* cf) {
     if (!bc_ok(b[q])) return "unknown boundary condition type";
   if (cf->mode < FST_MODE_PLAIN_FP64 || cf->mode > FST_MODE_HYBRID) return "unknown mode";
   if (cf->audit_every < 0 || cf->classify_every < 0) return "negative audit / classify period";
+  if (cf->grid_type != FST_GRID_CARTESIAN && cf->grid_type != FST_GRID_GENERALIZED)
+    return "unknown grid type";
+  if (cf->scheme < 0 || cf->scheme > FST_SCHEME_QUICK) return "unknown advection scheme";
+  if (cf->ndim == 2 && cf->scheme > FST_SCHEME_WENO5 && cf->mode != FST_MODE_PLAIN_FP64)
+    return "the centered4 and quick schemes run in FST_MODE_PLAIN_FP64";
+  if (cf->grid_type == FST_GRID_GENERALIZED) {
+    if (cf->mode != FST_MODE_PLAIN_FP64) return "generalized grids run in FST_MODE_PLAIN_FP64";
+    // the reference's gen2d / gen3d modules exchange no halo and apply no
+    // boundary conditions, so a periodic axis has no meaning there
+    if (cf->xper || cf->yper || (cf->ndim == 3 && cf->zper))
+      return "periodic axes are not supported on generalized grids";
+  }
   long long ngi = cf->nci + 6LL, ngj = cf->ncj + 6LL, ngk = cf->ndim == 3 ? cf->nck + 6LL : 1;
   if (ngi * ngj * ngk > (1LL << 40)) return "grid too large";
   return "";
@@ -111,9 +125,12 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
   P.ns = g.ns;
   P.nv = g.nv;
   P.nvt = g.nvt;
-  P.visc = cf.visc != 0;
-  P.ceq = cf.ceq != 0;
-  P.buoyancy = cf.buoyancy != 0;
+  // gen2d / gen3d compute advection and the pressure gradient only
+  const bool cart = cf.grid_type != FST_GRID_GENERALIZED;
+  P.visc = cart && cf.visc != 0;
+  P.ceq = cart && cf.ceq != 0;
+  P.buoyancy = cart && cf.buoyancy != 0;
+  P.scheme = g.ndim == 2 && cf.scheme > 0 ? cf.scheme : FST_SCHEME_WENO5;
   // device config array of the reference (src/cart3d.cpp:152-171)
   std::vector<double> cd(6 + 3 * g.ns, 0.0);
   for (int s = 0; s < g.ns; ++s) {
@@ -160,6 +177,7 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
     P.dxmag2 = P.dx * P.dx + P.dy * P.dy;
     P.dxmag = std::sqrt(P.dx * P.dx + P.dy * P.dy);
   }
+  if (!cart && g.ndim == 3) P.ddz = make_div(P.dx);  // calculateFluxesG(..., cf.dx, cf.dy, cf.dx, v)
   P.mu2d = 2.928e-5;
   P.kheat2d = 0.026;
   P.rd_f[0] = (float)(1.0 / P.dx);
@@ -188,15 +206,19 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
 // Device bytes of the work arrays of each path, in doubles per cell.
 size_t work_doubles_per_cell(const fst_config& cf, const Geo& g) {
   size_t w = 0;
+  const bool gen = cf.grid_type == FST_GRID_GENERALIZED;
+  const bool visc = cf.visc && !gen, ceq = cf.ceq && !gen;
   if (cf.mode == FST_MODE_PLAIN_FP64) {
     if (g.ndim == 3) {
       w = 2 + 3 + 1 + 1 + (size_t)3 * g.nv;  // rho p vel T nrg F
-      if (cf.visc) w += g.ns + 18;
-      if (cf.ceq) w += 27;
+      if (visc) w += g.ns + 18;
+      if (ceq) w += 27;
+      if (gen) w += 9;
     } else {
       w = 2 + 2 + 1 + 1 + (size_t)2 * g.nv;
-      if (cf.visc) w += 6 + 2;
-      if (cf.ceq) w += 8;
+      if (visc) w += 6 + 2;
+      if (ceq) w += 8;
+      if (gen) w += 4;
     }
   } else {
     w = fst_mixed_work_doubles_per_cell(cf, g);
@@ -378,6 +400,7 @@ int fst_create(const fst_config* cfg, fst_ctx** out) {
   if (!rc) rc = allocd(c, &c->Ua, nst);
   if (!rc) rc = allocd(c, &c->Ub, nst);
   if (!rc) rc = allocd(c, &c->dflag, 1);
+  c->gen = cfg->grid_type == FST_GRID_GENERALIZED;
   if (!rc && cfg->mode == FST_MODE_PLAIN_FP64 && g.ndim == 3) {
     Plain3DBufs& b = c->b3;
     rc = allocd(c, &b.rho, cells);
@@ -386,9 +409,10 @@ int fst_create(const fst_config* cfg, fst_ctx** out) {
     if (!rc) rc = allocd(c, &b.T, cells);
     if (!rc) rc = allocd(c, &b.nrg, cells);
     if (!rc) rc = allocd(c, &b.F, (size_t)3 * g.nv * cells);
-    if (!rc && cfg->visc) rc = allocd(c, &b.Y, (size_t)g.ns * cells);
-    if (!rc && cfg->visc) rc = allocd(c, &b.S, 18 * cells);
-    if (!rc && cfg->ceq) rc = allocd(c, &b.MF, 27 * cells);
+    if (!rc && c->P.visc) rc = allocd(c, &b.Y, (size_t)g.ns * cells);
+    if (!rc && c->P.visc) rc = allocd(c, &b.S, 18 * cells);
+    if (!rc && c->P.ceq) rc = allocd(c, &b.MF, 27 * cells);
+    if (!rc && c->gen) rc = allocd(c, &b.met, 9 * cells);
     if (!rc) rc = allocd(c, &b.red, 2);
   } else if (!rc && cfg->mode == FST_MODE_PLAIN_FP64) {
     Plain2DBufs& b = c->b2;
@@ -398,9 +422,10 @@ int fst_create(const fst_config* cfg, fst_ctx** out) {
     if (!rc) rc = allocd(c, &b.T, cells);
     if (!rc) rc = allocd(c, &b.nrg, cells);
     if (!rc) rc = allocd(c, &b.F, (size_t)2 * g.nv * cells);
-    if (!rc && cfg->visc) rc = allocd(c, &b.S, 6 * cells);
-    if (!rc && cfg->visc) rc = allocd(c, &b.Q, 2 * cells);
-    if (!rc && cfg->ceq) rc = allocd(c, &b.MF, 8 * cells);
+    if (!rc && c->P.visc) rc = allocd(c, &b.S, 6 * cells);
+    if (!rc && c->P.visc) rc = allocd(c, &b.Q, 2 * cells);
+    if (!rc && c->P.ceq) rc = allocd(c, &b.MF, 8 * cells);
+    if (!rc && c->gen) rc = allocd(c, &b.met, 4 * cells);
     if (!rc) rc = allocd(c, &b.red, 2);
   } else if (!rc) {
     std::string why;
@@ -515,8 +540,9 @@ int fst_compute_rhs(fst_ctx* c, double* R, size_t n) {
     e = cudaMemsetAsync(c->Rdev, 0, nst * sizeof(double), c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "rhs memset");
   }
+  if (c->gen && !c->grid_set) return fail(c, FST_ERR_INVALID, "fst_set_grid has not been called");
   int rc = FST_OK;
-  if (c->g.ndim == 3) rc = bcs(c, c->Ua);  // cart3d_func::compute applies BCs first
+  if (c->g.ndim == 3 && !c->gen) rc = bcs(c, c->Ua);  // cart3d_func::compute applies BCs first
   c->bm.stage = 0;
   c->bm.classified = false;
   if (!rc) rc = stage(c, c->Ua, c->Ua, nullptr, 0.0, c->Rdev, false);
@@ -531,15 +557,18 @@ int fst_compute_rhs(fst_ctx* c, double* R, size_t n) {
 
 int fst_rk_step(fst_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return FST_ERR_INVALID;
+  if (c->gen && !c->grid_set) return fail(c, FST_ERR_INVALID, "fst_set_grid has not been called");
   cudaEventRecord(c->ev0, c->stream);
   for (int s = 0; s < nsteps; ++s) {
     int rc = FST_OK;
     const bool two_d = c->g.ndim == 2;
-    if (two_d) rc = bcs(c, c->Ua);  // cart2d_func::preStep
-    if (!rc && !two_d) rc = bcs(c, c->Ua);
+    // gen2d / gen3d apply no boundary conditions (src/gen2d.cpp:132-134,
+    // src/gen3d.cpp:109, 338-370)
+    if (two_d && !c->gen) rc = bcs(c, c->Ua);  // cart2d_func::preStep
+    if (!rc && !two_d && !c->gen) rc = bcs(c, c->Ua);
     c->bm.stage = 1;
     if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, true);
-    if (!rc && !two_d) rc = bcs(c, c->Ub);
+    if (!rc && !two_d && !c->gen) rc = bcs(c, c->Ub);
     c->bm.stage = 2;
     if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
     if (rc) return rc;
@@ -549,6 +578,40 @@ int fst_rk_step(fst_ctx* c, int nsteps) {
   cudaEventRecord(c->ev1, c->stream);
   c->timed = nsteps > 0;
   return check_launch(c, "rk_step");
+}
+
+int fst_set_grid(fst_ctx* c, const double* nodes, size_t n) {
+  if (!c || !nodes) return FST_ERR_INVALID;
+  if (!c->gen) return fail(c, FST_ERR_UNSUPPORTED, "not a generalized-grid context");
+  if (n != fst_grid_size(&c->cf)) return fail(c, FST_ERR_SIZE, "grid size mismatch");
+  double* dX = nullptr;
+  cudaError_t e = cudaMalloc(&dX, n * sizeof(double));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, FST_ERR_OOM, "grid buffer allocation failed");
+  }
+  double* met = c->g.ndim == 3 ? c->b3.met : c->b2.met;
+  e = cudaMemcpyAsync(dX, nodes, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    c->stats.kernel_launches += fst_gen_metrics(c->g, dX, met, c->stream);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(dX);
+  if (e != cudaSuccess) return cuda_fail(c, e, "set_grid");
+  c->grid_set = true;
+  return FST_OK;
+}
+
+int fst_get_metrics(fst_ctx* c, double* out, size_t n) {
+  if (!c || !out) return FST_ERR_INVALID;
+  if (!c->gen) return fail(c, FST_ERR_UNSUPPORTED, "not a generalized-grid context");
+  if (n != fst_metrics_size(&c->cf)) return fail(c, FST_ERR_SIZE, "metrics size mismatch");
+  const double* met = c->g.ndim == 3 ? c->b3.met : c->b2.met;
+  cudaError_t e = cudaMemcpyAsync(out, met, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "get_metrics");
+  return FST_OK;
 }
 
 int fst_secondary(fst_ctx* c, double* out, size_t n) {
@@ -640,6 +703,7 @@ int fst_status(fst_ctx* c, double* vmin, double* vmax, double* xmin, double* xma
 
 int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
   if (!c || !np) return FST_ERR_INVALID;
+  if (c->gen) return fail(c, FST_ERR_UNSUPPORTED, "the noise filter runs on cartesian grids");
   if (np->nt < 0) return fail(c, FST_ERR_INVALID, "noise nt must be >= 0");
   const Geo& g = c->g;
   if (!c->dnoise) {  // zero-initialised like the module's FS3D_I / FS2D_I

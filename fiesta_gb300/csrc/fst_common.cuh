@@ -32,6 +32,7 @@ struct DivC {
 // Physics constants of one run, passed by value to the kernels.
 struct Phys {
   int ns, nv, nvt, visc, ceq, buoyancy;
+  int scheme;  // 2D flux: 1 WENO5, 2 centered4, 3 QUICK (src/cart2d.cpp:165-172)
   // species constants of calculateRhoPT (src/secondary.hpp:127-135):
   //   cp_s = gammas*Rs/(gammas-1), cv_s = Rs/(gammas-1), Rs = cd(7+3s)
   double cp_s[FST_MAX_SPECIES], cv_s[FST_MAX_SPECIES], mu_s[FST_MAX_SPECIES];

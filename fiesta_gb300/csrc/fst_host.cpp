@@ -143,6 +143,16 @@ size_t fst_state_size(const fst_config* c) {
   return g.cells() * (size_t)g.nvt;
 }
 
+size_t fst_grid_size(const fst_config* c) {
+  const size_t nk = c->ndim == 3 ? (size_t)c->nck + 1 : 1;
+  return ((size_t)c->nci + 1) * ((size_t)c->ncj + 1) * nk * 3;
+}
+
+size_t fst_metrics_size(const fst_config* c) {
+  Grid g(c);
+  return g.cells() * (size_t)(c->ndim == 3 ? 9 : 4);
+}
+
 int fst_fill_initial_conditions(const fst_config* c, const fst_ic_params* ic, double* U,
                                 size_t n) {
   if (!c || !ic || !U) return FST_ERR_INVALID;

@@ -59,6 +59,9 @@ struct Prof {
 // fst_api.cu
 std::string fst_setup_geo_phys(const fst_config* cfg, Geo& g, Phys& P);
 
+// fst_gen.cu: metric tensor of a generalized grid from its node coordinates
+int fst_gen_metrics(const Geo& g, const double* nodes, double* met, cudaStream_t st);
+
 // fst_bc.cu
 int fst_launch_bcs(const Geo& g, const fst_config& cf, double* U, cudaStream_t stream, Prof* prof);
 
@@ -67,6 +70,7 @@ struct Plain3DBufs {
   double *rho, *pr, *vel, *Y, *nrg, *T;
   double *F, *S, *MF;
   unsigned long long* red;
+  double* met;  // generalized grids: metric tensor (ngi,ngj,ngk,3,3), else null
 };
 int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* Uin,
                       const double* Uold, double* Unew, double coef, double* Rout, bool ghosts,
@@ -78,6 +82,7 @@ int fst_plain3d_secondary(const Geo& g, const Phys& P, const Plain3DBufs& b, con
 struct Plain2DBufs {
   double *rho, *pr, *vel, *T, *nrg;
   double *F, *S, *Q, *MF;
+  double* met;  // generalized grids: metric tensor (ngi,ngj,2,2), else null
   unsigned long long* red;
 };
 int fst_plain2d_stage(const Geo& g, const Phys& P, const Plain2DBufs& b, const double* Uin,

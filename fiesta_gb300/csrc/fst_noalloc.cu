@@ -57,8 +57,8 @@ extern "C" int fst_rhs2d_noalloc(const fst_config* cfg, const double* d_U, doubl
     std::fprintf(stderr, "fst_rhs2d_noalloc: %s\n", why.c_str());
     return FST_ERR_INVALID;
   }
-  if (g.ndim != 2 || cfg->mode != FST_MODE_PLAIN_FP64) {
-    std::fprintf(stderr, "fst_rhs2d_noalloc: needs a 2D plain FP64 config\n");
+  if (g.ndim != 2 || cfg->mode != FST_MODE_PLAIN_FP64 || cfg->grid_type != FST_GRID_CARTESIAN) {
+    std::fprintf(stderr, "fst_rhs2d_noalloc: needs a 2D cartesian plain FP64 config\n");
     return FST_ERR_UNSUPPORTED;
   }
   const size_t cells = (size_t)g.sv;

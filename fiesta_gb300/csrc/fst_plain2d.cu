@@ -1,5 +1,9 @@
 // fst_plain2d.cu — plain FP64 right-hand side of cart2d_func::compute
-// (src/cart2d.cpp:151-237) and the stage combine of rkAdvance for sm_103a.
+// (src/cart2d.cpp:151-237) and gen2d_func::compute (src/gen2d.cpp:103-130),
+// and the stage combine of rkAdvance for sm_103a.  The flux pass carries the
+// three 2D schemes of both modules (WENO5, centered4, QUICK); on generalized
+// grids the primitive pass writes the contravariant velocity and the cell
+// pass applies the metric pressure gradient.
 //
 // Same structure as the 3D path: one pass for primitives and the three
 // C-equation maxima, one pass for WENO fluxes, one pass for the viscous and
@@ -24,7 +28,8 @@ __global__ void __launch_bounds__(256) k_prim2d(Geo g, Phys P, const double* __r
                                                 double* __restrict__ rho, double* __restrict__ pr,
                                                 double* __restrict__ vel, double* __restrict__ T,
                                                 double* __restrict__ nrg,
-                                                unsigned long long* __restrict__ red) {
+                                                unsigned long long* __restrict__ red,
+                                                const double* __restrict__ met) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long sv = g.sv;
   double lS = -1.7976931348623157e308, lC = -1.7976931348623157e308;
@@ -47,8 +52,15 @@ __global__ void __launch_bounds__(256) k_prim2d(Geo g, Phys P, const double* __r
     const double u = m0 / r, v = m1 / r;
     rho[c] = r;
     pr[c] = p;
-    vel[c] = u;
-    vel[c + sv] = v;
+    if (met) {
+      // computeGenVelocity2D (src/velocity.hpp:49-66), metric (a,b) at
+      // met[c + sv*(a + 2b)]
+      vel[c] = met[c] * m0 / r + met[c + 2 * sv] * m1 / r;
+      vel[c + sv] = met[c + sv] * m0 / r + met[c + 3 * sv] * m1 / r;
+    } else {
+      vel[c] = u;
+      vel[c + sv] = v;
+    }
     if (T) T[c] = p / ((Cp - Cv) * r);
     if (nrg) nrg[c] = E / r - 0.5 * r * (u * u + v * v);
     if (red) {
@@ -102,6 +114,7 @@ __device__ __forceinline__ double weno2d(double f1, double f2, double f3, double
 // computeFluxWeno2D::operator() (src/flux.hpp:65-105) for all v < nv,
 // face box [ng-1, ngi-ng) x [ng-1, ngj-ng).  F[(dir*nv + v)*sv + cell].
 __global__ void __launch_bounds__(128) k_flux2d(Geo g, Phys P, const double* __restrict__ U,
+                                                const double* __restrict__ rho,
                                                 const double* __restrict__ pr,
                                                 const double* __restrict__ vel,
                                                 double* __restrict__ F) {
@@ -110,6 +123,30 @@ __global__ void __launch_bounds__(128) k_flux2d(Geo g, Phys P, const double* __r
   if (i >= g.ngi - g.ng || j >= g.ngj - g.ng) return;
   const long long c = fst_idx(g, i, j, 0);
   const long long sv = g.sv;
+  if (P.scheme == FST_SCHEME_CENTERED4) {
+    // computeFluxCentered2D (src/flux.hpp:108-167): fourth-order centred
+    // face values; face velocity from var(., dir) / rho, p added for the
+    // energy only
+#pragma unroll 1
+    for (int dir = 0; dir < 2; ++dir) {
+      const long long s = dir == 0 ? 1 : g.sy;
+      const double* m = U + sv * dir;
+      const double uf = (0.0 - m[c + 2 * s] / rho[c + 2 * s] + 7.0 * m[c + s] / rho[c + s] +
+                         7.0 * m[c] / rho[c] - m[c - s] / rho[c - s]) /
+                        12.0;
+      const double pf = (0.0 - pr[c + 2 * s] + 7.0 * pr[c + s] + 7.0 * pr[c] - pr[c - s]) / 12.0;
+      const DivC dd = dir == 0 ? P.ddx : P.ddy;
+      double* Fd = F + (long long)dir * P.nv * sv;
+#pragma unroll 1
+      for (int v = 0; v < P.nv; ++v) {
+        const double* q = U + sv * v;
+        double x1 = (0.0 - q[c + 2 * s] + 7.0 * q[c + s] + 7.0 * q[c] - q[c - s]) / 12.0;
+        if (v == 2) x1 = x1 + pf;
+        Fd[sv * v + c] = dd(uf * x1);
+      }
+    }
+    return;
+  }
 #pragma unroll 1
   for (int dir = 0; dir < 2; ++dir) {
     const long long s = dir == 0 ? 1 : g.sy;
@@ -126,6 +163,17 @@ __global__ void __launch_bounds__(128) k_flux2d(Geo g, Phys P, const double* __r
       f1 = q[c0]; f2 = q[c0 + o]; f3 = q[c0 + 2 * o]; f4 = q[c0 + 3 * o]; f5 = q[c0 + 4 * o];
       const double p1 = pr[c0], p2 = pr[c0 + o], p3 = pr[c0 + 2 * o], p4 = pr[c0 + 3 * o],
                    p5 = pr[c0 + 4 * o];
+      if (P.scheme == FST_SCHEME_QUICK) {
+        // computeFluxQuick2D (src/flux.hpp:169-221): three upwind values
+        // f1 = q(c0+o), f2 = q(c0+2o), f3 = q(c0+3o) of the same stencil
+        if (v == 2) {
+          f2 = f2 + p2; f3 = f3 + p3; f4 = f4 + p4;
+        } else if (!(fst_finite(p2) && fst_finite(p3) && fst_finite(p4))) {
+          f2 = f2 + 0.0 * p2; f3 = f3 + 0.0 * p3; f4 = f4 + 0.0 * p4;
+        }
+        Fd[sv * v + c] = dd(uf * (0.75 * f3 + 0.375 * f4 - 0.125 * f2));
+        continue;
+      }
       if (v == 2) {
         f1 = f1 + p1; f2 = f2 + p2; f3 = f3 + p3; f4 = f4 + p4; f5 = f5 + p5;
       } else if (!(fst_finite(p1) && fst_finite(p2) && fst_finite(p3) && fst_finite(p4) &&
@@ -229,7 +277,8 @@ __global__ void __launch_bounds__(128) k_cell2d(Geo g, Phys P, const double* __r
                                                 const double* __restrict__ MF,
                                                 const unsigned long long* __restrict__ red,
                                                 const double* Uold, double* Unew, double coef,
-                                                double* __restrict__ Rout) {
+                                                double* __restrict__ Rout,
+                                                const double* __restrict__ met) {
   const int i = g.ng + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = g.ng + blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.ngi - g.ng || j >= g.ngj - g.ng) return;
@@ -247,7 +296,17 @@ __global__ void __launch_bounds__(128) k_cell2d(Geo g, Phys P, const double* __r
   };
   double R0 = divF(0), R1 = divF(1), R2 = divF(2);
   for (int v = 3; v < nv; ++v) emit(v, divF(v));
-  {
+  if (met) {
+    // applyGenPressureGradient2D (src/presgrad.hpp:148-190)
+    auto d4m = [&](long long st, int a, int w) {
+      const double* m = met + sv * (a + 2 * w);
+      return (pr[c - 2 * st] * m[c - 2 * st] - 8.0 * pr[c - st] * m[c - st] +
+              8.0 * pr[c + st] * m[c + st] - pr[c + 2 * st] * m[c + 2 * st]) /
+             12.0;
+    };
+    R0 = R0 - (d4m(sx, 0, 0) + d4m(sy, 1, 0));
+    R1 = R1 - (d4m(sx, 0, 1) + d4m(sy, 1, 1));
+  } else {
     const double dxp = (pr[c - 2 * sx] - 8.0 * pr[c - sx] + 8.0 * pr[c + sx] - pr[c + 2 * sx]) / P.d12x;
     const double dyp = (pr[c - 2 * sy] - 8.0 * pr[c - sy] + 8.0 * pr[c + sy] - pr[c + 2 * sy]) / P.d12y;
     R0 -= dxp;
@@ -331,6 +390,10 @@ __global__ void __launch_bounds__(128) k_cell2d(Geo g, Phys P, const double* __r
       else R1 += diffu;
     }
   }
+  // C-equation variables carried without a right-hand side (the generalized
+  // module evolves none): U + coef*0, as the reference's zero dvar gives
+  if (!P.ceq)
+    for (int v = nv; v < g.nvt; ++v) emit(v, 0.0);
   emit(0, R0);
   emit(1, R1);
   emit(2, R2);
@@ -365,10 +428,11 @@ int fst_plain2d_stage(const Geo& g, const Phys& P, const Plain2DBufs& b, const d
              k_prim2d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel,
                                                        P.visc ? b.T : nullptr,
                                                        P.ceq ? b.nrg : nullptr,
-                                                       P.ceq ? b.red : nullptr));
+                                                       P.ceq ? b.red : nullptr, b.met));
   const dim3 bf(32, 4, 1);
   const dim3 gf(cdiv(g.nci + 1, 32), cdiv(g.ncj + 1, 4), 1);
-  FST_LAUNCH(prof, "flux2d", st, n, k_flux2d<<<gf, bf, 0, st>>>(g, P, Uin, b.pr, b.vel, b.F));
+  FST_LAUNCH(prof, "flux2d", st, n,
+             k_flux2d<<<gf, bf, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel, b.F));
   if (P.visc || P.ceq) {
     FST_LAUNCH(prof, "faces2d", st, n,
                k_faces2d<<<gf, bf, 0, st>>>(g, P, Uin, b.rho, b.vel, b.T, b.red, b.S, b.Q, b.MF));
@@ -376,7 +440,7 @@ int fst_plain2d_stage(const Geo& g, const Phys& P, const Plain2DBufs& b, const d
   const dim3 gc(cdiv(g.nci, 32), cdiv(g.ncj, 4), 1);
   FST_LAUNCH(prof, "cell2d", st, n,
              k_cell2d<<<gc, bf, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel, b.nrg, b.F, b.S, b.Q,
-                                         b.MF, b.red, Uold, Unew, coef, Rout));
+                                         b.MF, b.red, Uold, Unew, coef, Rout, b.met));
   if (ghosts && !Rout) {
     FST_LAUNCH(prof, "ghost2d", st, n,
                k_ghost2d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, Uold, Unew, coef));
@@ -386,6 +450,7 @@ int fst_plain2d_stage(const Geo& g, const Phys& P, const Plain2DBufs& b, const d
 
 int fst_plain2d_secondary(const Geo& g, const Phys& P, const Plain2DBufs& b, const double* U,
                           cudaStream_t st) {
-  k_prim2d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, P, U, b.rho, b.pr, b.vel, b.T, nullptr, nullptr);
+  k_prim2d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, P, U, b.rho, b.pr, b.vel, b.T, nullptr, nullptr,
+                                            nullptr);
   return 1;
 }

@@ -1,6 +1,9 @@
 // fst_plain3d.cu — plain FP64 right-hand side of cart3d_func::compute
-// (src/cart3d.cpp:220-298) and the rkAdvance stage combine (src/rk.cpp:28-70)
-// for sm_103a.
+// (src/cart3d.cpp:220-298) and gen3d_func::compute (src/gen3d.cpp:338-370),
+// and the rkAdvance stage combine (src/rk.cpp:28-70) for sm_103a.  On
+// generalized grids the primitive pass writes the contravariant velocity and
+// the cell pass applies the metric pressure gradient; the flux pass is the
+// same WENO5 with the reference's dz = cf.dx (src/gen3d.cpp:359).
 //
 // The reference runs ~41 Kokkos launches per stage with every intermediate in
 // HBM.  Here a stage is four kernels:
@@ -35,7 +38,8 @@ __global__ void __launch_bounds__(256) k_prim3d(Geo g, Phys P, const double* __r
                                                 double* __restrict__ rho, double* __restrict__ pr,
                                                 double* __restrict__ vel, double* __restrict__ Y,
                                                 double* __restrict__ nrg, double* __restrict__ T,
-                                                unsigned long long* __restrict__ red) {
+                                                unsigned long long* __restrict__ red,
+                                                const double* __restrict__ met) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long sv = g.sv;
   double lS = -1.7976931348623157e308, lC = -1.7976931348623157e308;
@@ -55,9 +59,19 @@ __global__ void __launch_bounds__(256) k_prim3d(Geo g, Phys P, const double* __r
     const double u = m0 / r, v = m1 / r, w = m2 / r;
     rho[c] = r;
     pr[c] = p;
-    vel[c] = u;
-    vel[c + sv] = v;
-    vel[c + 2 * sv] = w;
+    if (met) {
+      // computeGenVelocity3D (src/velocity.hpp:23-48): contravariant velocity
+      // sum_b m(a,b) * var(b) / rho, metric (a,b) at met[c + sv*(a + 3b)]
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double* M = met + c + sv * a;
+        vel[c + sv * a] = M[0] * m0 / r + M[3 * sv] * m1 / r + M[6 * sv] * m2 / r;
+      }
+    } else {
+      vel[c] = u;
+      vel[c + sv] = v;
+      vel[c + 2 * sv] = w;
+    }
     if (T) T[c] = p / ((Cp - Cv) * r);
     // specific internal energy of calculateRhoGrad::nrg (src/ceq3d.hpp:137-141)
     if (nrg) nrg[c] = E / r - 0.5 * r * (u * u + v * v + w * w);
@@ -262,7 +276,8 @@ __global__ void __launch_bounds__(128) k_cell3d(Geo g, Phys P, const double* __r
                                                 const double* __restrict__ MF,
                                                 const unsigned long long* __restrict__ red,
                                                 const double* Uold, double* Unew, double coef,
-                                                double* __restrict__ Rout) {
+                                                double* __restrict__ Rout,
+                                                const double* __restrict__ met) {
   const int i = g.ng + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = g.ng + blockIdx.y * blockDim.y + threadIdx.y;
   const int k = g.ng + blockIdx.z;
@@ -286,7 +301,19 @@ __global__ void __launch_bounds__(128) k_cell3d(Geo g, Phys P, const double* __r
   // species: only the advective term
   for (int v = 4; v < nv; ++v) emit(v, divF(v));
 
-  {  // pressure gradient; the reference uses dz = cd(2) for the z term
+  if (met) {
+    // applyGenPressureGradient3D (src/presgrad.hpp:72-146): fourth-order
+    // differences of p * m(a, w) along each computational direction a
+    auto d4m = [&](long long st, int a, int w) {
+      const double* m = met + sv * (a + 3 * w);
+      return (pr[c - 2 * st] * m[c - 2 * st] - 8.0 * pr[c - st] * m[c - st] +
+              8.0 * pr[c + st] * m[c + st] - pr[c + 2 * st] * m[c + 2 * st]) /
+             12.0;
+    };
+    R0 = R0 - (d4m(sx, 0, 0) + d4m(sy, 1, 0) + d4m(sz, 2, 0));
+    R1 = R1 - (d4m(sx, 0, 1) + d4m(sy, 1, 1) + d4m(sz, 2, 1));
+    R2 = R2 - (d4m(sx, 0, 2) + d4m(sy, 1, 2) + d4m(sz, 2, 2));
+  } else {  // pressure gradient; the reference uses dz = cd(2) for the z term
     const double dxp = (pr[c - 2 * sx] - 8.0 * pr[c - sx] + 8.0 * pr[c + sx] - pr[c + 2 * sx]) / P.d12x;
     const double dyp = (pr[c - 2 * sy] - 8.0 * pr[c - sy] + 8.0 * pr[c + sy] - pr[c + 2 * sy]) / P.d12y;
     const double dzp = (pr[c - 2 * sz] - 8.0 * pr[c - sz] + 8.0 * pr[c + sz] - pr[c + 2 * sz]) / P.d12pz;
@@ -380,6 +407,10 @@ __global__ void __launch_bounds__(128) k_cell3d(Geo g, Phys P, const double* __r
     R1 += diffu[1];
     R2 += diffu[2];
   }
+  // C-equation variables carried without a right-hand side (the generalized
+  // module evolves none): U + coef*0, as the reference's zero dvar gives
+  if (!P.ceq)
+    for (int v = nv; v < g.nvt; ++v) emit(v, 0.0);
   emit(0, R0);
   emit(1, R1);
   emit(2, R2);
@@ -419,7 +450,7 @@ int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const d
              k_prim3d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel,
                                                        P.visc ? b.Y : nullptr,
                                                        P.ceq ? b.nrg : nullptr, nullptr,
-                                                       P.ceq ? b.red : nullptr));
+                                                       P.ceq ? b.red : nullptr, b.met));
   const dim3 bf(32, 4, 1);
   const dim3 gf(cdiv(g.nci + 1, 32), cdiv(g.ncj + 1, 4), g.nck + 1);
   FST_LAUNCH(prof, "flux3d", st, n, k_flux3d<<<gf, bf, 0, st>>>(g, P, Uin, b.pr, b.vel, b.F));
@@ -430,7 +461,7 @@ int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const d
   const dim3 gc(cdiv(g.nci, 32), cdiv(g.ncj, 4), g.nck);
   FST_LAUNCH(prof, "cell3d", st, n,
              k_cell3d<<<gc, bf, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel, b.nrg, b.F, b.S, b.MF,
-                                         b.red, Uold, Unew, coef, Rout));
+                                         b.red, Uold, Unew, coef, Rout, b.met));
   if (ghosts && !Rout)
     FST_LAUNCH(prof, "ghost3d", st, n,
                k_ghost3d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, Uold, Unew, coef));
@@ -441,6 +472,6 @@ int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const d
 int fst_plain3d_secondary(const Geo& g, const Phys& P, const Plain3DBufs& b, const double* U,
                           cudaStream_t st) {
   k_prim3d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, P, U, b.rho, b.pr, b.vel, nullptr, nullptr, b.T,
-                                            nullptr);
+                                            nullptr, nullptr);
   return 1;
 }

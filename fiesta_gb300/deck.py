@@ -845,13 +845,18 @@ class Deck:
     def config(self):
         """The fst_config of this deck (abi.FstConfig)."""
         n = list(self.ni) + [1] * (3 - len(self.ni))
+        gen = self.grid == "generalized"
+        # generalized grids run in computational space: dx = dy = dz = 1
+        # (src/input.cpp:344-350)
+        dx = [1.0, 1.0, 1.0] if gen else list(self.dx) + [self.dx[0]] * (3 - len(self.dx))
         return abi.make_config(self.ndim, n, dt=self.dt, species=self.species, R=self.R,
                                visc=self.visc, ceq=self.ceq, kap=self.kap, eps=self.eps,
                                alpha=self.alpha, buoyancy=self.buoyancy, g=self.g_accel,
                                rho_ref=self.rho_ref, periodic=self.periodic,
                                bcs=self.bcs, mode=self.mode, audit_every=self.audit_every,
-                               dx=list(self.dx) + [self.dx[0]] * (3 - len(self.dx)),
-                               classify_every=self.classify_every)
+                               dx=dx, classify_every=self.classify_every,
+                               grid_type=abi.GRID_GENERALIZED if gen else abi.GRID_CARTESIAN,
+                               scheme=_SCHEMES.get(self.scheme, abi.SCHEME_WENO5))
 
     def noise_params(self):
         """abi.FstNoiseParams of fiesta.noise, or None when the filter is off."""
@@ -860,33 +865,87 @@ class Deck:
         return abi.FstNoiseParams(dh=self.noise_dh, eta=self.noise_eta, coff=self.noise_coff,
                                   nt=self.noise_nt, mode=self.noise_mode)
 
-    def initial_conditions(self, cfg=None):
-        """Evaluate ``fiesta.initial_conditions(x, y, z, v)`` at every interior
-        cell centre, as loadInitialConditions (src/input.cpp:453-515): uniform
-        grids, x = dx*(i-ng) + 0.5*dx, conserved variables v < nv only; ghosts
-        and C-variables stay zero.  Interpreted Python: for modest grids."""
+    def _call_number(self, name, args):
+        """luaReader::call (src/luaReader.cpp:317-345): fiesta.<name>(...)
+        must exist and return a number."""
+        fn = _fiesta(self.lua).get(name)
+        if fn is None:
+            raise DeckError(f"Could not find fiesta.{name} in '{self.filename}'")
+        r = self.lua.call(fn, args)
+        val = r[0] if r else None
+        try:
+            return float(_num(val, "conversion"))
+        except DeckError:
+            raise DeckError(f"function '{name}' should return a number") from None
+
+    def grid_nodes(self, cfg=None):
+        """Node coordinates of a generalized grid, (ni, nj, nk, 3) with
+        ni = nci + 1: ``fiesta.initialize_grid(i, j, k, v)`` for v < ndim at
+        every node, as loadGrid (src/input.cpp:529-560) on one rank."""
         import numpy as np
         cfg = cfg or self.config()
-        fn = _fiesta(self.lua).get("initial_conditions")
-        if fn is None:
-            raise DeckError(f"Could not find fiesta.initial_conditions in '{self.filename}'")
+        ni, nj, nk, _ = abi.grid_dims(cfg)
+        X = np.zeros((ni, nj, nk, 3), order="F")
+        for v in range(cfg.ndim):
+            for k in range(nk):
+                for j in range(nj):
+                    for i in range(ni):
+                        X[i, j, k, v] = self._call_number(
+                            "initialize_grid", [float(i), float(j), float(k), float(v)])
+        return X
+
+    def initial_conditions(self, cfg=None, nodes=None):
+        """Evaluate ``fiesta.initial_conditions(x, y, z, v)`` at every interior
+        cell centre, as loadInitialConditions (src/input.cpp:453-515): uniform
+        grids, x = dx*(i-ng) + 0.5*dx; generalized grids, the mean of the
+        cell's nodes (``nodes`` from grid_nodes(), computed when not given);
+        conserved variables v < nv only; ghosts and C-variables stay zero.
+        Interpreted Python: for modest grids."""
+        import numpy as np
+        cfg = cfg or self.config()
+        gen = cfg.grid_type == abi.GRID_GENERALIZED
+        if gen and nodes is None:
+            nodes = self.grid_nodes(cfg)
         ngi, ngj, ngk, nvt = abi.dims(cfg)
         nv = abi.nv_of(cfg)
         ng = cfg.ng
         U = np.zeros((ngi, ngj, ngk, nvt), order="F")
         ks = range(ng, cfg.nck + ng) if cfg.ndim == 3 else [0]
+
+        def centre(i, j, k):
+            if not gen:
+                x = cfg.dx * (i - ng) + 0.5 * cfg.dx
+                y = cfg.dy * (j - ng) + 0.5 * cfg.dy
+                z = cfg.dz * (k - ng) + 0.5 * cfg.dz if cfg.ndim == 3 else 0.0
+                return x, y, z
+            x = y = z = 0.0
+            if cfg.ndim == 3:
+                for ix in range(2):
+                    for iy in range(2):
+                        for iz in range(2):
+                            a, b, c = i + ix - ng, j + iy - ng, k + iz - ng
+                            x += nodes[a, b, c, 0]
+                            y += nodes[a, b, c, 1]
+                            z += nodes[a, b, c, 2]
+                return x / 8.0, y / 8.0, z / 8.0
+            for ix in range(2):
+                for iy in range(2):
+                    x += nodes[i + ix - ng, j + iy - ng, 0, 0]
+                    y += nodes[i + ix - ng, j + iy - ng, 0, 1]
+            return x / 4.0, y / 4.0, 0.0
+
         for v in range(nv):
             for k in ks:
-                z = cfg.dz * (k - ng) + 0.5 * cfg.dz if cfg.ndim == 3 else 0.0
                 for j in range(ng, cfg.ncj + ng):
-                    y = cfg.dy * (j - ng) + 0.5 * cfg.dy
                     for i in range(ng, cfg.nci + ng):
-                        x = cfg.dx * (i - ng) + 0.5 * cfg.dx
-                        r = self.lua.call(fn, [x, y, z, float(v)])
-                        val = r[0] if r else None
-                        U[i, j, k, v] = float(_num(val, "conversion")) if val is not None \
-                            else 0.0
+                        x, y, z = centre(i, j, k)
+                        U[i, j, k, v] = self._call_number("initial_conditions",
+                                                          [x, y, z, float(v)])
         return U
+
+
+_SCHEMES = {"weno5": abi.SCHEME_WENO5, "centered4": abi.SCHEME_CENTERED4,
+            "quick": abi.SCHEME_QUICK}
 
 
 def _fiesta(lua):
@@ -1049,11 +1108,24 @@ def load(path=None, text=None):
 
 
 def _check_supported(d):
-    """What the library's right-hand side covers: uniform Cartesian WENO5."""
-    if d.grid != "cartesian":
-        raise DeckError(f"fiesta.grid.type '{d.grid}' is not supported (cartesian only)")
-    if d.scheme != "weno5":
-        raise DeckError(f"fiesta.advection_scheme '{d.scheme}' is not supported (weno5 only)")
+    """What the library's right-hand side covers: cartesian and generalized
+    grids; the three 2D advection schemes (an unknown scheme name leaves
+    WENO5, as src/input.cpp:317-323 does); the 3D modules use WENO5."""
+    if d.grid == "terrain":
+        raise DeckError("fiesta.grid.type 'terrain' is not supported (it reads a terrain "
+                        "file through the HDF5 writer)")
+    if d.grid not in ("cartesian", "generalized"):
+        raise DeckError(f"unknown fiesta.grid.type '{d.grid}'")
+    if d.grid == "generalized":
+        if d.mode != abi.MODE_PLAIN_FP64:
+            raise DeckError("generalized grids run in the plain FP64 mode")
+        if any(d.periodic[:d.ndim]):
+            raise DeckError("periodic axes are not supported on generalized grids")
+        if d.noise:
+            raise DeckError("the noise filter runs on cartesian grids")
+    if (d.ndim == 2 and _SCHEMES.get(d.scheme, 1) != abi.SCHEME_WENO5
+            and d.mode != abi.MODE_PLAIN_FP64):
+        raise DeckError(f"fiesta.advection_scheme '{d.scheme}' runs in the plain FP64 mode")
     if d.ng != 3:
         raise DeckError("fiesta.ng must be 3")
     if not d.species:

@@ -45,6 +45,10 @@ _EXPORTS = {
     "fst_secondary": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_check_finite": (C.c_int, [C.c_void_p]),
     "fst_noise_filter": (C.c_int, [C.c_void_p, C.POINTER(abi.FstNoiseParams)]),
+    "fst_grid_size": (C.c_size_t, [C.POINTER(abi.FstConfig)]),
+    "fst_metrics_size": (C.c_size_t, [C.POINTER(abi.FstConfig)]),
+    "fst_set_grid": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
+    "fst_get_metrics": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                              C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fst_get_stats": (C.c_int, [C.c_void_p, C.POINTER(abi.FstStats)]),
@@ -153,6 +157,20 @@ class Solver:
 
     def get_state_device(self, ptr):
         self._check(lib().fst_get_state_device(self._ctx, C.c_void_p(ptr), self.n), "get_state_device")
+
+    # -- generalized grids ----------------------------------------------
+    def set_grid(self, nodes):
+        """Node coordinates (ni, nj, nk, 3) of a generalized grid; computes
+        the metric tensor on every cell (loadGrid + preSim of gen2d/gen3d)."""
+        X = np.asfortranarray(nodes, dtype=np.float64)
+        if X.shape != abi.grid_dims(self.cfg):
+            raise ValueError(f"grid shape {X.shape} != {abi.grid_dims(self.cfg)}")
+        self._check(lib().fst_set_grid(self._ctx, _dptr(X), X.size), "set_grid")
+
+    def metrics(self):
+        out = np.zeros(abi.metrics_dims(self.cfg), dtype=np.float64, order="F")
+        self._check(lib().fst_get_metrics(self._ctx, _dptr(out), out.size), "get_metrics")
+        return out
 
     # -- the path ------------------------------------------------------
     def apply_bcs(self):

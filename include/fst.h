@@ -1,7 +1,8 @@
 /*
  * fst.h — C ABI of libfst, the GB300 (sm_103a) implementation of FIESTA's
- * per-Runge-Kutta-stage right-hand side and update for uniform Cartesian
- * grids (the cart2d / cart3d modules).
+ * per-Runge-Kutta-stage right-hand side and update: uniform Cartesian grids
+ * (the cart2d / cart3d modules) and generalized curvilinear grids (the
+ * gen2d / gen3d modules).
  *
  * Everything crossing this boundary is plain C: a config struct, pointers and
  * sizes.  No C++, Kokkos or torch types appear in any signature.
@@ -70,6 +71,22 @@ enum {
                               smooth faces to the linear upwind flux        */
 };
 
+/* Grid type (fiesta.grid.type, src/input.cpp:287-350).  GENERALIZED runs the
+ * reference's gen2d / gen3d modules (src/gen2d.cpp, src/gen3d.cpp): curvilinear
+ * node coordinates given by fst_set_grid, metric terms on every cell. */
+enum {
+  FST_GRID_CARTESIAN = 0,
+  FST_GRID_GENERALIZED = 1
+};
+
+/* 2D advection scheme (fiesta.advection_scheme, src/input.cpp:317-323); the
+ * 3D modules always use WENO5.  0 means WENO5. */
+enum {
+  FST_SCHEME_WENO5 = 1,
+  FST_SCHEME_CENTERED4 = 2, /* computeFluxCentered2D (src/flux.hpp:108-167) */
+  FST_SCHEME_QUICK = 3      /* computeFluxQuick2D (src/flux.hpp:169-221)    */
+};
+
 /*
  * Run configuration: the fields of the reference's `struct inputConfig`
  * (src/input.hpp:59-148) that the RHS path reads, filled from the same Lua
@@ -97,7 +114,9 @@ typedef struct fst_config {
   int mode;                  /* FST_MODE_*                                  */
   int audit_every;           /* HYBRID: full-WENO audit step period (0: never) */
   int classify_every;        /* HYBRID: steps between classifications (0, 1: every step) */
-  int reserved[7];           /* zero                                        */
+  int grid_type;             /* FST_GRID_* (fiesta.grid.type)               */
+  int scheme;                /* FST_SCHEME_* (fiesta.advection_scheme), 0 = WENO5 */
+  int reserved[5];           /* zero                                        */
 } fst_config;
 
 /* Per-context statistics (fst_stats). */
@@ -152,15 +171,18 @@ int fst_get_state_device(fst_ctx* ctx, double* d_U, size_t n);
 int fst_apply_bcs(fst_ctx* ctx);
 
 /* One right-hand-side evaluation of the current state: replaces
- * cart3d_func::compute (src/cart3d.cpp:220-298, which applies BCs first) and
- * cart2d_func::compute (src/cart2d.cpp:151-237, which does not).  If R is not
- * NULL the RHS `dvar` (LayoutLeft, zero outside the interior) is copied to it.
- * n = fst_state_size(). */
+ * cart3d_func::compute (src/cart3d.cpp:220-298, which applies BCs first),
+ * cart2d_func::compute (src/cart2d.cpp:151-237, which does not), and on
+ * generalized grids gen3d_func::compute / gen2d_func::compute
+ * (src/gen3d.cpp:338-370, src/gen2d.cpp:103-130: no BCs, no viscous, buoyancy
+ * or C-equation terms).  If R is not NULL the RHS `dvar` (LayoutLeft, zero
+ * outside the interior) is copied to it.  n = fst_state_size(). */
 int fst_compute_rhs(fst_ctx* ctx, double* R, size_t n);
 
-/* `nsteps` time steps: each is preStep (2D: applyBCs, src/cart2d.cpp:147-149)
- * followed by rkAdvance (src/rk.cpp:28-70): two RHS evaluations and the two
- * stage combines. */
+/* `nsteps` time steps: each is preStep (cartesian 2D: applyBCs,
+ * src/cart2d.cpp:147-149; nothing on generalized grids) followed by
+ * rkAdvance (src/rk.cpp:28-70): two RHS evaluations and the two stage
+ * combines. */
 int fst_rk_step(fst_ctx* ctx, int nsteps);
 
 /* Secondary variables of the current state over all cells, replacing
@@ -201,8 +223,28 @@ typedef struct fst_noise_params {
  * of a sweep in loop order (i slowest); this entry point reproduces that
  * order exactly (tile wavefronts), giving the reference's serial result bit
  * for bit.  The noise indicator persists between calls, as the module's
- * member array does. */
+ * member array does.  Cartesian grids only (FST_ERR_UNSUPPORTED otherwise). */
 int fst_noise_filter(fst_ctx* ctx, const fst_noise_params* np);
+
+/* Node coordinates of a generalized grid: (ni, nj, nk, 3) doubles, LayoutLeft,
+ * ni = nci + 1, nj = ncj + 1, nk = nck + 1 in 3D and 1 in 2D (the reference's
+ * `grid` view, src/gen3d.cpp:41, src/gen2d.cpp:25; filled by loadGrid,
+ * src/input.cpp:529-560).  The 2D third component is ignored. */
+size_t fst_grid_size(const fst_config* cfg);
+
+/* Load the node coordinates and compute the metric tensor on every cell:
+ * replaces loadGrid + gen3d_func::preSim / gen2d_func::preSim
+ * (src/gen3d.cpp:129-335, src/gen2d.cpp:190-320): computeMetrics3D/2D
+ * (src/metric.hpp:22-166) on the interior, then the ghost layers mirrored
+ * from the interior in the reference's order.  Required before the first
+ * right-hand side of an FST_GRID_GENERALIZED context. */
+int fst_set_grid(fst_ctx* ctx, const double* nodes, size_t n);
+
+/* The metric tensor of a generalized context, LayoutLeft:
+ * 3D (ngi, ngj, ngk, 3, 3), 2D (ngi, ngj, 2, 2) — the reference's `metrics`
+ * view.  n = fst_metrics_size(). */
+size_t fst_metrics_size(const fst_config* cfg);
+int fst_get_metrics(fst_ctx* ctx, double* out, size_t n);
 
 /* Per-kernel device timing (the reference's per-region fiestaTimer,
  * src/timer.hpp:52-119, reset/accumulated around kernels in

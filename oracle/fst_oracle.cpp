@@ -8,7 +8,10 @@
 // It restates, in plain serial/OpenMP C++, the reference's FP64 kernel
 // sequence operation for operation:
 //   - cart3d_func::compute      (src/cart3d.cpp:220-298)
-//   - cart2d_func::compute      (src/cart2d.cpp:151-237), preStep (:147-149)
+//   - cart2d_func::compute      (src/cart2d.cpp:151-237), preStep (:147-149),
+//                               with the WENO5 / centred / QUICK 2D fluxes
+//   - gen3d_func::compute / gen2d_func::compute (src/gen3d.cpp:338-370,
+//     src/gen2d.cpp:103-130) and their preSim metrics (src/metric.hpp)
 //   - rkAdvance                 (src/rk.cpp:28-70)
 //   - applyBCs / bc_gen / bc_*Per (src/bc.cpp:33-249)
 // Each kernel function below names the reference functor it follows.  The
@@ -25,6 +28,7 @@
 // (oracle/ref_build.sh), and against the reference's BC known-answer tests
 // (tests/bc_outflow.cpp, bc_reflective.cpp, bc_hydrostatic.cpp, test.cpp).
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -55,6 +59,13 @@ struct Oracle {
   std::vector<double> qx, qy;            // 2D heat flux
   std::vector<double> gradRho;           // 3D: 5 comps, 2D: 4 comps
   std::vector<double> mFlux;             // 3D: (3,3,i,j,k,3), 2D m: (2,2,i,j,2)
+  // generalized grids (src/gen3d.cpp, src/gen2d.cpp)
+  bool gen = false;
+  int scheme = 1;                        // 2D advection scheme (cf.scheme)
+  double fdz = 1;                        // dz passed to calculateFluxesG
+  std::vector<double> met;               // (i,j,k,a,b), a,b < ndim
+  std::vector<double> nodes;             // (ni,nj,nk,3), LayoutLeft as given
+  int ni = 0, nj = 0, nk = 0;
   double last_maxS = 0, last_maxCh = 0;
   std::string err;
 
@@ -142,6 +153,17 @@ struct Oracle {
       cd[8 + 3 * s] = cf.mu[s];
     }
     dxmag = dx * dx + dy * dy + dz * dz;
+    gen = cf.grid_type == FST_GRID_GENERALIZED;
+    scheme = ndim == 2 && cf.scheme > 0 ? cf.scheme : 1;
+    fdz = gen ? dx : dz;  // gen3d passes cf.dx as dz (src/gen3d.cpp:359)
+    if (gen) {             // the modules compute advection and pressure only
+      cf.visc = 0;
+      cf.ceq = 0;
+      cf.buoyancy = 0;
+    }
+    ni = nci + 1;
+    nj = ncj + 1;
+    nk = ndim == 3 ? nck + 1 : 1;
     size_t nc = (size_t)ngi * ngj * ngk;
     var.assign(nc * nvt, 0.0);
     tmp1.assign(nc * nvt, 0.0);
@@ -150,6 +172,7 @@ struct Oracle {
     vel.assign(nc * ndim, 0.0);
     fluxx.assign(nc, 0.0); fluxy.assign(nc, 0.0);
     if (ndim == 3) fluxz.assign(nc, 0.0);
+    if (gen) met.assign(nc * ndim * ndim, 0.0);
     if (cf.visc) {
       if (ndim == 3) stress.assign(nc * 6, 0.0);
       else { stressx.assign(nc * 4, 0.0); stressy.assign(nc * 4, 0.0);
@@ -341,8 +364,8 @@ struct Oracle {
     f4 = q(i, j, k); f5 = q(i, j, k - 1); f6 = q(i, j, k - 2);
     wr = (-VEL(i, j, k + 2, 2) + 7.0f * VEL(i, j, k + 1, 2) + 7.0f * VEL(i, j, k, 2) -
           VEL(i, j, k - 1, 2)) / 12.0f;
-    if (wr < 0.0) fluxz[c3(i, j, k)] = wr * weno3(f1, f2, f3, f4, f5) / dz;
-    else          fluxz[c3(i, j, k)] = wr * weno3(f6, f5, f4, f3, f2) / dz;
+    if (wr < 0.0) fluxz[c3(i, j, k)] = wr * weno3(f1, f2, f3, f4, f5) / fdz;
+    else          fluxz[c3(i, j, k)] = wr * weno3(f6, f5, f4, f3, f2) / fdz;
   }
   // advect3D (src/advect.hpp:39-61)
   void advect3D(int i, int j, int k, int v) {
@@ -827,7 +850,7 @@ struct Oracle {
     box(0, ngi, 0, ngj, 0, 1, [&](int i, int j, int) { rhoPT2D(i, j); });
     box(0, ngi, 0, ngj, 0, 1, [&](int i, int j, int) { velocity2D(i, j); });
     for (int v = 0; v < nv; ++v) {
-      box(b - 1, ei, b - 1, ej, 0, 1, [&](int i, int j, int) { fluxes2D(i, j, v); });
+      box(b - 1, ei, b - 1, ej, 0, 1, [&](int i, int j, int) { flux2D_any(i, j, v); });
       box(b, ei, b, ej, 0, 1, [&](int i, int j, int) { advect2D(i, j, v); });
     }
     box(b, ei, b, ej, 0, 1, [&](int i, int j, int) { presgrad2D(i, j); });
@@ -851,14 +874,223 @@ struct Oracle {
     }
   }
 
+  // ==================================================================
+  // 2D centred and QUICK fluxes (cf.scheme 2 and 3), src/flux.hpp:108-221
+  // ==================================================================
+  // computeFluxCentered2D::operator() (src/flux.hpp:121-166)
+  void fluxCentered2D(int i, int j, int v) {
+    double ur, vr, x1, y1, px, py;
+    ur = (0.0 - V(i + 2, j, 0, 0) / RHO(i + 2, j, 0) + 7.0 * V(i + 1, j, 0, 0) / RHO(i + 1, j, 0) +
+          7.0 * V(i, j, 0, 0) / RHO(i, j, 0) - V(i - 1, j, 0, 0) / RHO(i - 1, j, 0)) / 12.0;
+    vr = (0.0 - V(i, j + 2, 0, 1) / RHO(i, j + 2, 0) + 7.0 * V(i, j + 1, 0, 1) / RHO(i, j + 1, 0) +
+          7.0 * V(i, j, 0, 1) / RHO(i, j, 0) - V(i, j - 1, 0, 1) / RHO(i, j - 1, 0)) / 12.0;
+    px = (0.0 - P(i + 2, j, 0) + 7.0 * P(i + 1, j, 0) + 7.0 * P(i, j, 0) - P(i - 1, j, 0)) / 12.0;
+    py = (0.0 - P(i, j + 2, 0) + 7.0 * P(i, j + 1, 0) + 7.0 * P(i, j, 0) - P(i, j - 1, 0)) / 12.0;
+    x1 = (0.0 - V(i + 2, j, 0, v) + 7.0 * V(i + 1, j, 0, v) + 7.0 * V(i, j, 0, v) - V(i - 1, j, 0, v)) / 12.0;
+    y1 = (0.0 - V(i, j + 2, 0, v) + 7.0 * V(i, j + 1, 0, v) + 7.0 * V(i, j, 0, v) - V(i, j - 1, 0, v)) / 12.0;
+    if (v == 2) {
+      x1 = x1 + px;
+      y1 = y1 + py;
+    }
+    fluxx[c3(i, j, 0)] = ur * x1 / cd[1];
+    fluxy[c3(i, j, 0)] = vr * y1 / cd[2];
+  }
+  // computeFluxQuick2D::operator() (src/flux.hpp:187-220)
+  void fluxQuick2D(int i, int j, int v) {
+    auto q = [&](int a, int b) { return V(a, b, 0, v) + (v == 2) * P(a, b, 0); };
+    auto quick = [](double f1, double f2, double f3) { return 0.75 * f2 + 0.375 * f3 - 0.125 * f1; };
+    double ur = (-VEL(i + 2, j, 0, 0) + 7.0 * VEL(i + 1, j, 0, 0) + 7.0 * VEL(i, j, 0, 0) - VEL(i - 1, j, 0, 0)) / 12.0;
+    double f1, f2, f3;
+    if (ur < 0.0) { f1 = q(i + 2, j); f2 = q(i + 1, j); f3 = q(i, j); }
+    else          { f1 = q(i - 1, j); f2 = q(i, j); f3 = q(i + 1, j); }
+    fluxx[c3(i, j, 0)] = ur * quick(f1, f2, f3) / cd[1];
+    double vr = (-VEL(i, j + 2, 0, 1) + 7.0 * VEL(i, j + 1, 0, 1) + 7.0 * VEL(i, j, 0, 1) - VEL(i, j - 1, 0, 1)) / 12.0;
+    if (vr < 0.0) { f1 = q(i, j + 2); f2 = q(i, j + 1); f3 = q(i, j); }
+    else          { f1 = q(i, j - 1); f2 = q(i, j); f3 = q(i, j + 1); }
+    fluxy[c3(i, j, 0)] = vr * quick(f1, f2, f3) / cd[2];
+  }
+  void flux2D_any(int i, int j, int v) {
+    if (scheme == 3) fluxQuick2D(i, j, v);
+    else if (scheme == 2) fluxCentered2D(i, j, v);
+    else fluxes2D(i, j, v);
+  }
+
+  // ==================================================================
+  // Generalized grids: src/metric.hpp, src/gen3d.cpp, src/gen2d.cpp
+  // ==================================================================
+  inline double X(int ii, int jj, int kk, int d) const {
+    return nodes[(size_t)ii + (size_t)ni * (jj + (size_t)nj * (kk + (size_t)nk * d))];
+  }
+  inline double& MT(int i, int j, int k, int a, int b) {
+    return met[(c3(i, j, k) * ndim + a) * ndim + b];
+  }
+  // computeMetrics3D::operator() (src/metric.hpp:62-164), written out term by term
+  void metrics3D(int i, int j, int k) {
+    const int a = i - 3, b = j - 3, c = k - 3;
+    double fm[3][3], fp[3][3];  // [face axis][component]: centroid of the - / + face
+    for (int d = 0; d < 3; ++d) {
+      fm[0][d] = (X(a, b, c, d) + X(a, b + 1, c, d) + X(a, b, c + 1, d) + X(a, b + 1, c + 1, d)) / 4.0;
+      fp[0][d] = (X(a + 1, b, c, d) + X(a + 1, b + 1, c, d) + X(a + 1, b, c + 1, d) + X(a + 1, b + 1, c + 1, d)) / 4.0;
+      fm[2][d] = (X(a, b, c, d) + X(a + 1, b, c, d) + X(a, b + 1, c, d) + X(a + 1, b + 1, c, d)) / 4.0;
+      fp[2][d] = (X(a, b, c + 1, d) + X(a + 1, b, c + 1, d) + X(a, b + 1, c + 1, d) + X(a + 1, b + 1, c + 1, d)) / 4.0;
+      fm[1][d] = (X(a, b, c, d) + X(a + 1, b, c, d) + X(a, b, c + 1, d) + X(a + 1, b, c + 1, d)) / 4.0;
+      fp[1][d] = (X(a, b + 1, c, d) + X(a + 1, b + 1, c, d) + X(a, b + 1, c + 1, d) + X(a + 1, b + 1, c + 1, d)) / 4.0;
+    }
+    const double xxi = fp[0][0] - fm[0][0], xet = fp[1][0] - fm[1][0], xzt = fp[2][0] - fm[2][0];
+    const double yxi = fp[0][1] - fm[0][1], yet = fp[1][1] - fm[1][1], yzt = fp[2][1] - fm[2][1];
+    const double zxi = fp[0][2] - fm[0][2], zet = fp[1][2] - fm[1][2], zzt = fp[2][2] - fm[2][2];
+    const double jac = 1.0 / (xxi * (yet * zzt - yzt * zet) + xet * (yzt * zxi - yxi * zzt) +
+                              xzt * (yxi * zet - yet * zxi));
+    MT(i, j, k, 0, 0) = jac * (yet * zzt - yzt * zet);
+    MT(i, j, k, 0, 1) = jac * (xzt * zet - xet * zzt);
+    MT(i, j, k, 0, 2) = jac * (xet * yzt - xzt * yet);
+    MT(i, j, k, 1, 0) = jac * (yzt * zxi - yxi * zzt);
+    MT(i, j, k, 1, 1) = jac * (xxi * zzt - xzt * zxi);
+    MT(i, j, k, 1, 2) = jac * (xzt * yxi - xxi * yzt);
+    MT(i, j, k, 2, 0) = jac * (yxi * zet - yet * zxi);
+    MT(i, j, k, 2, 1) = jac * (xet * zxi - xxi * zet);
+    MT(i, j, k, 2, 2) = jac * (xxi * yet - xet * yxi);
+  }
+  // computeMetrics2D::operator() (src/metric.hpp:30-53)
+  void metrics2D(int i, int j) {
+    const int a = i - 3, b = j - 3;
+    double x_xi = (X(a + 1, b, 0, 0) + X(a + 1, b + 1, 0, 0)) / 2.0 - (X(a, b, 0, 0) + X(a, b + 1, 0, 0)) / 2.0;
+    double y_xi = (X(a + 1, b, 0, 1) + X(a + 1, b + 1, 0, 1)) / 2.0 - (X(a, b, 0, 1) + X(a, b + 1, 0, 1)) / 2.0;
+    double x_et = (X(a, b + 1, 0, 0) + X(a + 1, b + 1, 0, 0)) / 2.0 - (X(a, b, 0, 0) + X(a + 1, b, 0, 0)) / 2.0;
+    double y_et = (X(a, b + 1, 0, 1) + X(a + 1, b + 1, 0, 1)) / 2.0 - (X(a, b, 0, 1) + X(a + 1, b, 0, 1)) / 2.0;
+    double jac = 1.0 / (x_xi * y_et - x_et * y_xi);
+    MT(i, j, 0, 0, 0) = jac * y_et;
+    MT(i, j, 0, 0, 1) = -jac * x_et;
+    MT(i, j, 0, 1, 0) = -jac * y_xi;
+    MT(i, j, 0, 1, 1) = jac * x_xi;
+  }
+  // gen3d_func::preSim / gen2d_func::preSim metric setup: interior from the
+  // nodes, then the single-rank ghost mirrors (src/gen3d.cpp:278-331 in the
+  // order x-, x+, y-, y+, z-, z+; src/gen2d.cpp:280-317 in the order
+  // y-, y+, x-, x+), each over the full extent of the other axes.
+  void set_grid(const double* X_, size_t n) {
+    nodes.assign(X_, X_ + n);
+    std::fill(met.begin(), met.end(), 0.0);
+    if (ndim == 3)
+      box(ng, ngi - ng, ng, ngj - ng, ng, ngk - ng, [&](int i, int j, int k) { metrics3D(i, j, k); });
+    else
+      box(ng, ngi - ng, ng, ngj - ng, 0, 1, [&](int i, int j, int) { metrics2D(i, j); });
+    const int nm = ndim;
+    auto copy = [&](int di, int dj, int dk, int si, int sj, int sk) {
+      for (int a = 0; a < nm; ++a)
+        for (int b = 0; b < nm; ++b) MT(di, dj, dk, a, b) = MT(si, sj, sk, a, b);
+    };
+    auto mirror_x = [&](int side) {
+      for (int g = 0; g < ng; ++g)
+        for (int j = 0; j < ngj; ++j)
+          for (int k = 0; k < ngk; ++k) {
+            if (side == 0) copy(ng - g - 1, j, k, ng + g, j, k);
+            else copy(ngi - 1 - g, j, k, nci + g, j, k);
+          }
+    };
+    auto mirror_y = [&](int side) {
+      for (int i = 0; i < ngi; ++i)
+        for (int g = 0; g < ng; ++g)
+          for (int k = 0; k < ngk; ++k) {
+            if (side == 0) copy(i, ng - g - 1, k, i, ng + g, k);
+            else copy(i, ngj - 1 - g, k, i, ncj + g, k);
+          }
+    };
+    auto mirror_z = [&](int side) {
+      for (int i = 0; i < ngi; ++i)
+        for (int j = 0; j < ngj; ++j)
+          for (int g = 0; g < ng; ++g) {
+            if (side == 0) copy(i, j, ng - g - 1, i, j, ng + g);
+            else copy(i, j, ngk - 1 - g, i, j, nck + g);
+          }
+    };
+    if (ndim == 3) {
+      mirror_x(0); mirror_x(1); mirror_y(0); mirror_y(1); mirror_z(0); mirror_z(1);
+    } else {
+      mirror_y(0); mirror_y(1); mirror_x(0); mirror_x(1);
+    }
+  }
+  // computeGenVelocity3D (src/velocity.hpp:23-48)
+  void genVelocity3D(int i, int j, int k) {
+    for (int a = 0; a < 3; ++a)
+      VEL(i, j, k, a) = (MT(i, j, k, a, 0) * V(i, j, k, 0) / RHO(i, j, k) +
+                         MT(i, j, k, a, 1) * V(i, j, k, 1) / RHO(i, j, k) +
+                         MT(i, j, k, a, 2) * V(i, j, k, 2) / RHO(i, j, k));
+  }
+  // computeGenVelocity2D (src/velocity.hpp:49-66)
+  void genVelocity2D(int i, int j) {
+    for (int a = 0; a < 2; ++a)
+      VEL(i, j, 0, a) = (MT(i, j, 0, a, 0) * V(i, j, 0, 0) / RHO(i, j, 0) +
+                         MT(i, j, 0, a, 1) * V(i, j, 0, 1) / RHO(i, j, 0));
+  }
+  // applyGenPressureGradient3D (src/presgrad.hpp:84-145)
+  void genPresgrad3D(int i, int j, int k) {
+    for (int w = 0; w < 3; ++w) {
+      double dxi = (P(i - 2, j, k) * MT(i - 2, j, k, 0, w) - 8.0 * P(i - 1, j, k) * MT(i - 1, j, k, 0, w) +
+                    8.0 * P(i + 1, j, k) * MT(i + 1, j, k, 0, w) - P(i + 2, j, k) * MT(i + 2, j, k, 0, w)) / (12.0);
+      double det = (P(i, j - 2, k) * MT(i, j - 2, k, 1, w) - 8.0 * P(i, j - 1, k) * MT(i, j - 1, k, 1, w) +
+                    8.0 * P(i, j + 1, k) * MT(i, j + 1, k, 1, w) - P(i, j + 2, k) * MT(i, j + 2, k, 1, w)) / (12.0);
+      double dzt = (P(i, j, k - 2) * MT(i, j, k - 2, 2, w) - 8.0 * P(i, j, k - 1) * MT(i, j, k - 1, 2, w) +
+                    8.0 * P(i, j, k + 1) * MT(i, j, k + 1, 2, w) - P(i, j, k + 2) * MT(i, j, k + 2, 2, w)) / (12.0);
+      D(i, j, k, w) = (D(i, j, k, w) - (dxi + det + dzt));
+    }
+  }
+  // applyGenPressureGradient2D (src/presgrad.hpp:160-189)
+  void genPresgrad2D(int i, int j) {
+    for (int w = 0; w < 2; ++w) {
+      double dxi = (P(i - 2, j, 0) * MT(i - 2, j, 0, 0, w) - 8.0 * P(i - 1, j, 0) * MT(i - 1, j, 0, 0, w) +
+                    8.0 * P(i + 1, j, 0) * MT(i + 1, j, 0, 0, w) - P(i + 2, j, 0) * MT(i + 2, j, 0, 0, w)) / (12.0);
+      double det = (P(i, j - 2, 0) * MT(i, j - 2, 0, 1, w) - 8.0 * P(i, j - 1, 0) * MT(i, j - 1, 0, 1, w) +
+                    8.0 * P(i, j + 1, 0) * MT(i, j + 1, 0, 1, w) - P(i, j + 2, 0) * MT(i, j + 2, 0, 1, w)) / (12.0);
+      D(i, j, 0, w) = (D(i, j, 0, w) - (dxi + det));
+    }
+  }
+  // gen3d_func::compute (src/gen3d.cpp:338-370): no BCs
+  void computeGen3D() {
+    const int b = ng, ei = ngi - ng, ej = ngj - ng, ek = ngk - ng;
+    box(0, ngi, 0, ngj, 0, ngk, [&](int i, int j, int k) { rhoPT3D(i, j, k); });
+    box(0, ngi, 0, ngj, 0, ngk, [&](int i, int j, int k) { genVelocity3D(i, j, k); });
+    for (int v = 0; v < nv; ++v) {
+      box(b - 1, ei, b - 1, ej, b - 1, ek, [&](int i, int j, int k) { fluxes3D(i, j, k, v); });
+      box(b, ei, b, ej, b, ek, [&](int i, int j, int k) { advect3D(i, j, k, v); });
+    }
+    box(b, ei, b, ej, b, ek, [&](int i, int j, int k) { genPresgrad3D(i, j, k); });
+  }
+  // gen2d_func::compute (src/gen2d.cpp:103-130)
+  void computeGen2D() {
+    const int b = ng, ei = ngi - ng, ej = ngj - ng;
+    box(0, ngi, 0, ngj, 0, 1, [&](int i, int j, int) { rhoPT2D(i, j); });
+    box(0, ngi, 0, ngj, 0, 1, [&](int i, int j, int) { genVelocity2D(i, j); });
+    for (int v = 0; v < nv; ++v) {
+      box(b - 1, ei, b - 1, ej, 0, 1, [&](int i, int j, int) { flux2D_any(i, j, v); });
+      box(b, ei, b, ej, 0, 1, [&](int i, int j, int) { advect2D(i, j, v); });
+    }
+    box(b, ei, b, ej, 0, 1, [&](int i, int j, int) { genPresgrad2D(i, j); });
+  }
+  void get_metrics(double* out) {
+    const size_t nc = (size_t)ngi * ngj * ngk;
+    for (int b = 0; b < ndim; ++b)
+      for (int a = 0; a < ndim; ++a)
+        for (int k = 0; k < ngk; ++k)
+          for (int j = 0; j < ngj; ++j)
+            for (int i = 0; i < ngi; ++i)
+              out[(size_t)i + (size_t)ngi * (j + (size_t)ngj * k) + nc * (a + (size_t)ndim * b)] =
+                  MT(i, j, k, a, b);
+  }
+
   void compute() {
+    if (gen) {
+      if (ndim == 3) computeGen3D();
+      else computeGen2D();
+      return;
+    }
     if (ndim == 3) compute3D();
     else compute2D();
   }
 
   // rkAdvance (src/rk.cpp:28-70), preceded by preStep.
   void rk_step() {
-    if (ndim == 2) apply_bcs();  // cart2d_func::preStep (src/cart2d.cpp:147-149)
+    if (ndim == 2 && !gen) apply_bcs();  // cart2d_func::preStep (src/cart2d.cpp:147-149)
     compute();
     const size_t n = var.size();
     const double hdt = 0.5f * dt;
@@ -1095,6 +1327,20 @@ int orc_get_noise(orc_ctx* c, int* out, size_t n) {
       for (int i = 0; i < o.ngi; ++i)
         out[(size_t)i + (size_t)o.ngi * (j + (size_t)o.ngj * k)] =
             o.noise.empty() ? 0 : o.noise[o.c3(i, j, k)];
+  return FST_OK;
+}
+int orc_set_grid(orc_ctx* c, const double* nodes, size_t n) {
+  Oracle& o = c->o;
+  if (!o.gen) return FST_ERR_UNSUPPORTED;
+  if (n != (size_t)o.ni * o.nj * o.nk * 3) return FST_ERR_SIZE;
+  o.set_grid(nodes, n);
+  return FST_OK;
+}
+int orc_get_metrics(orc_ctx* c, double* out, size_t n) {
+  Oracle& o = c->o;
+  if (!o.gen) return FST_ERR_UNSUPPORTED;
+  if (n != o.met.size()) return FST_ERR_SIZE;
+  o.get_metrics(out);
   return FST_OK;
 }
 int orc_set_threads(int n) {

@@ -117,6 +117,17 @@ class _Checker:
         self._call("get_noise", out.ctypes.data_as(C.POINTER(C.c_int)), C.c_size_t(out.size))
         return out
 
+    def set_grid(self, nodes):
+        """Node coordinates (ni, nj, nk, 3), Fortran order; computes the metrics."""
+        X = np.asfortranarray(nodes, dtype=np.float64)
+        self._call("set_grid", self._ptr(X), C.c_size_t(X.size))
+
+    def metrics(self):
+        d = self.cfg.ndim
+        out = np.zeros(self.shape[:3] + (d, d), dtype=np.float64, order="F")
+        self._call("get_metrics", self._ptr(out), C.c_size_t(out.size))
+        return out
+
     def secondary(self):
         nf = 6 if self.cfg.ndim == 3 else 5
         shp = self.shape[:3] + (nf,)

@@ -1,6 +1,7 @@
 // ref_harness.cpp — C entry points around the reference's own cart2d_func /
-// cart3d_func / applyBCs / rkAdvance, compiled from the reference sources by
-// oracle/ref_build.sh into oracle/_ref/libfiesta_ref.so.
+// cart3d_func / gen2d_func / gen3d_func / applyBCs / rkAdvance, compiled from
+// the reference sources by oracle/ref_build.sh into
+// oracle/_ref/libfiesta_ref.so.
 //
 // TEST INFRASTRUCTURE ONLY: it produces the golden vectors under tests/golden
 // and cross-checks the oracle restatement; nothing in the product loads it.
@@ -45,6 +46,10 @@ struct ref_ctx {
   inputConfig cf;
   std::unique_ptr<rk_func> f;
 };
+
+// ref_gen.cpp
+rk_func* ref_new_gen(inputConfig& cf);
+size_t ref_gen_metrics(rk_func* f, int ndim, double* out, size_t n);
 
 extern "C" {
 
@@ -98,7 +103,11 @@ int ref_create(const fst_config* c, ref_ctx** out) {
   cf.yMinus = cf.yPlus = -1 + (int)cf.yPer;
   cf.zMinus = cf.zPlus = -1 + (int)cf.zPer;
   cf.t = 0;
-  if (c->ndim == 3) x->f.reset(new cart3d_func(cf));
+  cf.scheme = c->scheme > 0 ? c->scheme : 1;  // src/input.cpp:317-323
+  cf.grid = c->grid_type;
+  // module choice of src/main.cpp:40-50
+  if (cf.grid > 0) x->f.reset(ref_new_gen(cf));
+  else if (c->ndim == 3) x->f.reset(new cart3d_func(cf));
   else x->f.reset(new cart2d_func(cf));
   *out = x;
   return 0;
@@ -115,6 +124,19 @@ int ref_get_state(ref_ctx* x, double* U, size_t n) {
   if (n != x->f->var.size()) return FST_ERR_SIZE;
   std::memcpy(U, x->f->var.data(), n * sizeof(double));
   return 0;
+}
+// loadGrid's copy into f->grid (src/input.cpp:529-560), then preSim, which
+// computes the metrics (src/gen3d.cpp:129-335, src/gen2d.cpp:190-320).
+int ref_set_grid(ref_ctx* x, const double* X, size_t n) {
+  if (x->cf.grid == 0) return FST_ERR_UNSUPPORTED;
+  if (n != x->f->grid.size()) return FST_ERR_SIZE;
+  std::memcpy(x->f->grid.data(), X, n * sizeof(double));
+  x->f->preSim();
+  return 0;
+}
+int ref_get_metrics(ref_ctx* x, double* out, size_t n) {
+  if (x->cf.grid == 0) return FST_ERR_UNSUPPORTED;
+  return ref_gen_metrics(x->f.get(), x->cf.ndim, out, n) == n ? 0 : FST_ERR_SIZE;
 }
 int ref_apply_bcs(ref_ctx* x) {
   applyBCs(x->cf, x->f.get());

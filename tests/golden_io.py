@@ -47,3 +47,38 @@ def interior(cfg, A):
     if cfg.ndim == 3:
         return A[ng:-ng, ng:-ng, ng:-ng]
     return A[ng:-ng, ng:-ng]
+
+
+def wavy_nodes(cfg, amp=0.2, L=1.0):
+    """Node coordinates (ni, nj, nk, 3) of a smoothly distorted box: a uniform
+    grid of a domain of size L per axis whose nodes are displaced by up to
+    ``amp`` cell widths along every axis (positive Jacobian for amp < 0.3)."""
+    ni, nj, nk = cfg.nci + 1, cfg.ncj + 1, (cfg.nck + 1 if cfg.ndim == 3 else 1)
+    i, j, k = np.meshgrid(np.arange(ni), np.arange(nj), np.arange(nk), indexing="ij")
+    h = [L / cfg.nci, L / cfg.ncj, L / cfg.nck if cfg.ndim == 3 else 0.0]
+    u, v, w = i / cfg.nci, j / cfg.ncj, (k / cfg.nck if cfg.ndim == 3 else 0.0 * k)
+    tp = 2.0 * np.pi
+    X = np.zeros((ni, nj, nk, 3), dtype=np.float64, order="F")
+    X[..., 0] = L * u + amp * h[0] * np.sin(tp * v + 0.3) * np.cos(tp * w)
+    X[..., 1] = L * v + amp * h[1] * np.sin(tp * u + 1.1) * np.cos(tp * w + 0.2)
+    if cfg.ndim == 3:
+        X[..., 2] = L * w + amp * h[2] * np.sin(tp * u + 0.7) * np.sin(tp * v + 0.4)
+    return np.asfortranarray(X)
+
+
+class GenCase:
+    """A generalized-grid fixture: nodes X, metrics MT, state U0 (ghosts
+    filled), one right-hand side R1 and the state UN after `steps` steps."""
+
+    def __init__(self, path):
+        z = np.load(path)
+        self.meta = json.loads(str(z["meta"]))
+        self.name = self.meta["name"]
+        self.cfg = abi.config_from_dict(self.meta["config"])
+        self.steps = int(self.meta["steps"])
+        for key in ("X", "MT", "U0", "R1", "UN"):
+            setattr(self, key, np.asfortranarray(z[key]))
+
+
+def load_gen():
+    return [GenCase(p) for p in sorted(glob.glob(os.path.join(HERE, "golden", "gen", "*.npz")))]

@@ -110,7 +110,16 @@ def test_required_keys_and_errors():
     with pytest.raises(deck.DeckError, match="fiesta.bc.xmin"):
         deck.load(text=DECK_3D.replace("fiesta.bc.xperiodic = true", ""))
     with pytest.raises(deck.DeckError, match="not supported"):
-        deck.load(text=DECK_3D.replace('"weno5"', '"centered4"'))
+        deck.load(text=DECK_3D.replace('"cartesian"', '"terrain"'))
+    with pytest.raises(deck.DeckError, match="periodic"):
+        deck.load(text=DECK_3D.replace('"cartesian"', '"generalized"')
+                  .replace('mode = "mixed"', 'mode = "plain"'))
+    with pytest.raises(deck.DeckError, match="plain FP64"):
+        deck.load(text=DECK_3D.replace('"cartesian"', '"generalized"'))
+    d = deck.load(text=DECK_3D.replace('"weno5"', '"centered4"'))
+    assert d.config().scheme == abi.SCHEME_CENTERED4  # the 3D modules ignore it
+    d = deck.load(text=DECK_3D.replace('"weno5"', '"upwind"'))
+    assert d.config().scheme == abi.SCHEME_WENO5      # unknown names leave WENO5
     with pytest.raises(deck.DeckError, match="mode"):
         deck.load(text=DECK_3D.replace('mode = "mixed"', 'mode = "fast"'))
     with pytest.raises(deck.DeckError):
@@ -158,3 +167,54 @@ def test_reference_sample_decks():
                 deck.load(p)
             legacy += 1
     assert ok >= 5 and legacy >= 1
+
+
+DECK_GEN2D = """
+fiesta.title = "wavy channel"
+fiesta.species = {{name="air", gamma=1.4, M=0.02897, mu=2.928e-5}}
+fiesta.time.dt = 1e-6
+fiesta.grid.type = "generalized"
+fiesta.grid.ndim = 2
+fiesta.grid.ni = {6, 5}
+fiesta.grid.dx = {0.5, 0.5}
+fiesta.advection_scheme = "quick"
+fiesta.bc.xmin = "outflow"
+fiesta.bc.xmax = "outflow"
+fiesta.bc.ymin = "reflective"
+fiesta.bc.ymax = "outflow"
+fiesta.mpi.procs = {1, 1}
+function fiesta.initialize_grid(i, j, k, v)
+    local x = i * 10 / 6
+    local dh = 0.3 * math.sin(x * 2.0)
+    if v == 0 then return x end
+    return dh + (10 - dh) * (j * 10 / 5) / 10
+end
+function fiesta.initial_conditions(x, y, z, v)
+    if v == 2 then return 1e5 + x + 10 * y end
+    if v == 3 then return 1.0 end
+    return 0
+end
+"""
+
+
+def test_generalized_deck_grid_and_cell_centres():
+    d = deck.load(text=DECK_GEN2D)
+    cfg = d.config()
+    assert cfg.grid_type == abi.GRID_GENERALIZED and cfg.scheme == abi.SCHEME_QUICK
+    assert (cfg.dx, cfg.dy) == (1.0, 1.0)  # computational space
+    X = d.grid_nodes(cfg)
+    assert X.shape == (7, 6, 1, 3) and np.all(X[..., 2] == 0)
+    i, j = 4, 2
+    x = i * 10 / 6
+    assert X[i, j, 0, 0] == x
+    assert X[i, j, 0, 1] == pytest.approx(0.3 * math.sin(2 * x) + (10 - 0.3 * math.sin(2 * x)) * j / 5,
+                                          rel=1e-15)
+    U = d.initial_conditions(cfg, X)
+    ci, cj = 3 + 2, 3 + 1  # cell (2, 1): the mean of its four nodes
+    xc = (X[2, 1, 0, 0] + X[2, 2, 0, 0] + X[3, 1, 0, 0] + X[3, 2, 0, 0]) / 4.0
+    yc = (X[2, 1, 0, 1] + X[2, 2, 0, 1] + X[3, 1, 0, 1] + X[3, 2, 0, 1]) / 4.0
+    assert U[ci, cj, 0, 2] == pytest.approx(1e5 + xc + 10 * yc, rel=1e-15)
+    assert U[ci, cj, 0, 3] == 1.0 and np.all(U[:3] == 0)
+    bad = DECK_GEN2D.replace("return 0\nend", "end")
+    with pytest.raises(deck.DeckError, match="should return a number"):
+        deck.load(text=bad).initial_conditions(cfg, X)

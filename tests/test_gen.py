@@ -1,0 +1,202 @@
+"""Generalized (curvilinear) grids — the reference's gen2d / gen3d modules —
+and the 2D centered4 / QUICK advection schemes.
+
+CPU: the oracle restatement against golden vectors made by the reference's
+own sources (tests/golden/make_golden_gen.py), against the reference itself on
+random cases where its tree is present, and the configuration checks that
+need no GPU.  GPU (marked): the CUDA path against the same golden vectors and
+the oracle, bit for bit (IEEE equality; NaN where the reference gives NaN).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from fiesta_gb300 import abi
+from fiesta_gb300.solver import FstError, Solver, initial_conditions, lib
+from oracle.oracle import Oracle, Reference
+from tests.golden_io import load_gen, same, wavy_nodes
+
+GEN = abi.GRID_GENERALIZED
+UNIT = (1.0, 1.0, 1.0)
+
+
+@pytest.fixture(scope="module")
+def gen_cases():
+    cases = load_gen()
+    assert len(cases) >= 6
+    return cases
+
+
+def _run(make, c):
+    """(metrics, R1, UN) of fixture case c through a checker or the GPU."""
+    gen = c.cfg.grid_type == GEN
+    x = make(c.cfg)
+    x.set_state(c.U0)
+    MT = None
+    if gen:
+        x.set_grid(c.X)
+        MT = x.metrics()
+    R1 = x.compute_rhs()
+    x = make(c.cfg)
+    x.set_state(c.U0)
+    if gen:
+        x.set_grid(c.X)
+    x.rk_step(c.steps)
+    return MT, R1, x.get_state()
+
+
+def test_oracle_matches_golden(gen_cases):
+    for c in gen_cases:
+        MT, R1, UN = _run(Oracle, c)
+        if MT is not None:
+            assert same(MT, c.MT), c.name
+        assert same(R1, c.R1), c.name
+        assert same(UN, c.UN), c.name
+
+
+def _random_gen(seed, ndim):
+    rng = np.random.default_rng(seed)
+    ns = int(rng.integers(1, 4))
+    sp = [dict(gamma=float(rng.uniform(1.2, 1.7)), M=float(rng.uniform(0.5, 3.0)), mu=1e-5)
+          for _ in range(ns)]
+    n = tuple(int(x) for x in rng.integers(1, 11, size=3))
+    scheme = int(rng.integers(1, 4)) if ndim == 2 else 1
+    cfg = abi.make_config(ndim, n, dx=UNIT, dt=1e-4, species=sp, R=1.0, grid_type=GEN,
+                          scheme=scheme, ceq=bool(rng.integers(0, 2)))
+    return cfg, float(rng.uniform(0.0, 0.28))
+
+
+@pytest.mark.skipif(not Reference.available(), reason="reference checker not built")
+@pytest.mark.parametrize("seed", list(range(8)))
+def test_oracle_matches_reference_random(seed):
+    cfg, amp = _random_gen(seed, 2 + seed % 2)
+    X = wavy_nodes(cfg, amp=amp)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, seed)
+    r, o = Reference(cfg), Oracle(cfg)
+    for x in (r, o):
+        x.set_state(U0)
+        x.apply_bcs()
+        x.set_grid(X)
+    assert same(o.metrics(), r.metrics())
+    assert same(o.compute_rhs(), r.compute_rhs())
+    o.rk_step(2)
+    r.rk_step(2)
+    assert same(o.get_state(), r.get_state())
+
+
+@pytest.mark.skipif(not Reference.available(), reason="reference checker not built")
+def test_oracle_matches_reference_zero_ghosts():
+    """The modules apply no BCs: with the interior-only initial state that
+    loadInitialConditions writes, zero-density ghosts give NaN near the
+    boundary in the reference, and the oracle reproduces where."""
+    cfg = abi.make_config(2, (9, 8), dx=UNIT, dt=1e-4, species=[dict(gamma=1.4, M=1.0)],
+                          R=1.0, grid_type=GEN)
+    X = wavy_nodes(cfg, amp=0.2)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 5)
+    r, o = Reference(cfg), Oracle(cfg)
+    for x in (r, o):
+        x.set_state(U0)
+        x.set_grid(X)
+    Rr, Ro = r.compute_rhs(), o.compute_rhs()
+    assert np.isnan(Rr).any() and same(Ro, Rr)
+
+
+def test_config_checks_without_gpu():
+    L = lib()
+    base = dict(dx=UNIT, dt=1e-4, R=1.0, grid_type=GEN)
+    bad = [abi.make_config(3, (4, 4, 4), periodic=(False, True, False), **base),
+           abi.make_config(3, (4, 4, 4), mode=abi.MODE_MIXED, **base),
+           abi.make_config(2, (4, 4), mode=abi.MODE_MIXED, scheme="quick", dx=UNIT),
+           abi.make_config(2, (4, 4), scheme=7, dx=UNIT)]
+    for cfg in bad:
+        with pytest.raises(FstError):
+            Solver(cfg)
+    cfg = abi.make_config(3, (4, 5, 6), **base)
+    assert L.fst_grid_size(cfg) == 5 * 6 * 7 * 3
+    assert L.fst_metrics_size(cfg) == 10 * 11 * 12 * 9
+    cfg2 = abi.make_config(2, (4, 5), **base)
+    assert L.fst_grid_size(cfg2) == 5 * 6 * 1 * 3
+    assert L.fst_metrics_size(cfg2) == 10 * 11 * 4
+
+
+# --------------------------------------------------------------------- GPU
+@pytest.mark.gpu
+def test_gpu_matches_golden(gen_cases):
+    for c in gen_cases:
+        MT, R1, UN = _run(Solver, c)
+        if MT is not None:
+            assert same(MT, c.MT), c.name
+        assert same(R1, c.R1), (c.name, np.nanmax(np.abs(R1 - c.R1)))
+        assert same(UN, c.UN), c.name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", list(range(10)))
+def test_gpu_matches_oracle_random(seed):
+    cfg, amp = _random_gen(100 + seed, 2 + seed % 2)
+    X = wavy_nodes(cfg, amp=amp)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, seed)
+    o, g = Oracle(cfg), Solver(cfg)
+    for x in (o, g):
+        x.set_state(U0)
+        x.apply_bcs()
+        x.set_grid(X)
+    assert same(g.metrics(), o.metrics())
+    assert same(g.compute_rhs(), o.compute_rhs())
+    o.rk_step(3)
+    g.rk_step(3)
+    assert same(g.get_state(), o.get_state())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ndim,n", [(3, (40, 33, 29)), (2, (300, 260, 1))])
+def test_gpu_matches_oracle_medium(ndim, n):
+    cfg = abi.make_config(ndim, n, dx=UNIT, dt=2e-5,
+                          species=[dict(gamma=1.4, M=1.0), dict(gamma=1.6, M=0.4)], R=1.0,
+                          grid_type=GEN)
+    X = wavy_nodes(cfg, amp=0.25)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 9)
+    o, g = Oracle(cfg), Solver(cfg)
+    for x in (o, g):
+        x.set_state(U0)
+        x.apply_bcs()
+        x.set_grid(X)
+    o.rk_step(2)
+    g.rk_step(2)
+    assert same(g.get_state(), o.get_state())
+
+
+@pytest.mark.gpu
+def test_gpu_zero_ghosts_nan_pattern():
+    cfg = abi.make_config(3, (7, 6, 5), dx=UNIT, dt=1e-4, species=[dict(gamma=1.4, M=1.0)],
+                          R=1.0, grid_type=GEN)
+    X = wavy_nodes(cfg, amp=0.2)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 3)
+    o, g = Oracle(cfg), Solver(cfg)
+    for x in (o, g):
+        x.set_state(U0)
+        x.set_grid(X)
+    Ro, Rg = o.compute_rhs(), g.compute_rhs()
+    assert np.isnan(Ro).any() and same(Rg, Ro)
+
+
+@pytest.mark.gpu
+def test_gpu_generalized_call_order_and_limits():
+    cfg = abi.make_config(2, (6, 6), dx=UNIT, dt=1e-4, R=1.0, grid_type=GEN)
+    g = Solver(cfg)
+    with pytest.raises(FstError):
+        g.compute_rhs()  # before set_grid
+    with pytest.raises(FstError):
+        g.rk_step(1)
+    with pytest.raises((FstError, ValueError)):
+        g.set_grid(np.zeros((3, 3, 1, 3)))
+    X = np.asfortranarray(wavy_nodes(cfg))
+    rc = lib().fst_set_grid(g._ctx, X.ctypes.data_as(C.POINTER(C.c_double)), X.size - 1)
+    assert rc == abi.FST_ERR_SIZE
+    g.set_grid(wavy_nodes(cfg))
+    with pytest.raises(FstError):
+        g.noise_filter(1e-5, 1e-3)
+    c = Solver(abi.make_config(2, (6, 6)))
+    with pytest.raises(FstError):
+        c.set_grid(wavy_nodes(cfg))
