@@ -178,6 +178,12 @@ def algorithmic_bytes(kernel, cfg):
         # momenta and energy of U_new read and written
         "mmom3d": inner * (4 * (4 + 3 + visc + (5 if ceq else 0)) + 16 * 4),
     }
+    # generalized grids (plain FP64): primitives read the 9 metrics and write
+    # rho, p and the contravariant velocity; the cell pass reads the fluxes,
+    # p and the 9 metrics once each
+    if getattr(cfg, "grid_type", 0) == 1:
+        tab["prim3d"] = 8 * allc * (nv + 9 + 5)
+        tab["cell3d"] = 8 * inner * (3 * nv + 1 + 9 + 2 * nvt)
     tab["mspec3d_hybrid"] = tab["mspec3d"] + inner * 3
     tab["mmom3d_hybrid"] = tab["mmom3d"] + inner * 3
     return tab.get(kernel)
@@ -353,6 +359,92 @@ def run_batch2d(steps, warmup, ncases=64):
                         "C-equation, buoyancy; mixed precision; CUDA graph per step"}
 
 
+def gen3d_cfg(n, dt):
+    from fiesta_gb300 import abi
+    return abi.make_config(3, (n, n, n), dx=(1.0, 1.0, 1.0), dt=dt, species=SPECIES,
+                           grid_type=abi.GRID_GENERALIZED)
+
+
+def gen3d_state(cfg, L):
+    """The mixing case on a wavy grid of side L: interior from the seeded
+    generator, ghosts filled once by outflow mirrors (the generalized module
+    never fills them), and dt from the largest contravariant speed."""
+    from fiesta_gb300 import abi
+    from fiesta_gb300.grids import wavy_box
+    from fiesta_gb300.solver import initial_conditions
+    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, SEED, **IC_KW)
+    X = wavy_box(cfg, amp=0.25, L=L)
+    S = max_wave_speed(cfg, U0) * cfg.nci / L  # |u|+c in cells per second
+    return U0, X, 0.4 / S
+
+
+def run_gen3d(n, steps, warmup, peak_gbs, peak_kind):
+    """The generalized-grid module (gen3d_func::compute) on a wavy 1 m box,
+    plain FP64: Mcell-steps/s, the dominant kernel's roofline, and the CPU
+    oracle on a bounded sample of the same case."""
+    import torch
+    from fiesta_gb300.solver import Solver
+    cfg = gen3d_cfg(n, 1.0)
+    U0, X, dt = gen3d_state(cfg, 1.0)
+    cfg.dt = dt
+    s = Solver(cfg)
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream.cuda_stream)
+    s.set_state(U0)
+    s.apply_bcs()
+    s.set_grid(X)
+    for _ in range(warmup):
+        s.rk_step(1)
+    torch.cuda.synchronize()
+    l0 = s.stats()["kernel_launches"]
+    s.set_profiling(True)
+    s.kernel_times()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        s.rk_step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kt = s.kernel_times()
+    s.set_profiling(False)
+    launches = s.stats()["kernel_launches"] - l0
+    finite = s.check_finite()
+    s.close()
+    top = max(kt.items(), key=lambda kv: kv[1][1])
+    name, (nl, tot) = top
+    b = algorithmic_bytes(name, cfg)
+    ach = b / (tot / nl / 1e3) / 1e9
+    return {"value": n ** 3 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-steps/s",
+            "ms_per_step": ms / steps, "gpu_launches": launches, "finite": finite,
+            "dtype": "f64",
+            "workload": f"gen3d_func::compute on a wavy {n}^3 grid, 5 species, "
+                        "plain FP64 (bit-identical to the reference)",
+            "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
+            "roofline": {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak_gbs,
+                         "unit": "GB/s", "frac": ach / peak_gbs, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / nl}}
+
+
+def cpu_sample_gen3d(n_sample=96, steps=1):
+    """The CPU oracle's generalized 3D step on a bounded sample."""
+    from oracle.oracle import Oracle
+    cores = os.cpu_count() or 1
+    Oracle.set_threads(cores)
+    cfg = gen3d_cfg(n_sample, 1.0)
+    U0, X, dt = gen3d_state(cfg, 1.0)
+    cfg.dt = dt
+    o = Oracle(cfg)
+    o.set_state(U0)
+    o.apply_bcs()
+    o.set_grid(X)
+    t0 = time.perf_counter()
+    o.rk_step(steps)
+    el = time.perf_counter() - t0
+    return {"value": n_sample ** 3 * steps / el / 1e6, "unit": "Mcell-steps/s", "cores": cores,
+            "kind": "port", "sample": f"{steps} step(s) at {n_sample}^3 ({el:.1f} s)"}
+
+
 def accuracy_report(cfg, U0, finals, nsteps):
     """rel-L2 per conserved field over the interior, after the same steps:
     mixed and hybrid against the plain FP64 path (bit-identical to the
@@ -431,6 +523,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-gen", action="store_true")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -498,6 +591,11 @@ def main():
     if rank != 0:
         return
     batch = None if a.no_batch else run_batch2d(a.steps, a.warmup)
+    gen3d = None
+    if not a.no_gen:
+        gen3d = run_gen3d(n, a.steps, a.warmup, peak, peak_kind)
+        if not a.no_cpu:
+            gen3d["cpu_baseline"] = cpu_sample_gen3d()
     cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
@@ -521,6 +619,7 @@ def main():
         "e2e": r["e2e"], "gpu_launches": r["gpu_launches"],
         "modes": {m: {k: v for k, v in results[m].items() if k not in ("clocks",)} for m in modes},
         "batch2d": batch,
+        "gen3d": gen3d,
         "accuracy": accuracy,
     }
     print(json.dumps(line))

@@ -286,12 +286,56 @@ class _RkFunc:
         self.solver.synchronize()
 
 
-class Cart3D(_RkFunc):
+class _CartFunc(_RkFunc):
+    def __init__(self, cfg):
+        if cfg.grid_type != abi.GRID_CARTESIAN:
+            raise ValueError(f"{type(self).__name__} needs a cartesian grid (use Gen3D/Gen2D)")
+        super().__init__(cfg)
+
+
+class Cart3D(_CartFunc):
     ndim = 3
 
 
-class Cart2D(_RkFunc):
+class Cart2D(_CartFunc):
     ndim = 2
+
+
+class _GenFunc(_RkFunc):
+    """Mirror of gen3d_func / gen2d_func (src/gen3d.hpp, src/gen2d.hpp): the
+    node coordinates go into ``grid`` (ni, nj, nk, 3) as loadGrid fills the
+    module's view, preSim computes the metric tensor, and no step applies
+    boundary conditions."""
+
+    def __init__(self, cfg):
+        if cfg.grid_type != abi.GRID_GENERALIZED:
+            raise ValueError(f"{type(self).__name__} needs grid_type = GRID_GENERALIZED")
+        super().__init__(cfg)
+        self.grid = None
+
+    def preSim(self):
+        if self.grid is None:
+            raise ValueError("set the grid node coordinates before preSim")
+        self.solver.set_grid(self.grid)
+
+    @property
+    def metrics(self):
+        return self.solver.metrics()
+
+
+class Gen3D(_GenFunc):
+    ndim = 3
+
+
+class Gen2D(_GenFunc):
+    ndim = 2
+
+
+def module_for(cfg):
+    """The module class src/main.cpp:40-50 picks for a configuration."""
+    if cfg.grid_type == abi.GRID_GENERALIZED:
+        return Gen3D if cfg.ndim == 3 else Gen2D
+    return Cart3D if cfg.ndim == 3 else Cart2D
 
 
 def _is_bad(v):

@@ -50,20 +50,9 @@ def interior(cfg, A):
 
 
 def wavy_nodes(cfg, amp=0.2, L=1.0):
-    """Node coordinates (ni, nj, nk, 3) of a smoothly distorted box: a uniform
-    grid of a domain of size L per axis whose nodes are displaced by up to
-    ``amp`` cell widths along every axis (positive Jacobian for amp < 0.3)."""
-    ni, nj, nk = cfg.nci + 1, cfg.ncj + 1, (cfg.nck + 1 if cfg.ndim == 3 else 1)
-    i, j, k = np.meshgrid(np.arange(ni), np.arange(nj), np.arange(nk), indexing="ij")
-    h = [L / cfg.nci, L / cfg.ncj, L / cfg.nck if cfg.ndim == 3 else 0.0]
-    u, v, w = i / cfg.nci, j / cfg.ncj, (k / cfg.nck if cfg.ndim == 3 else 0.0 * k)
-    tp = 2.0 * np.pi
-    X = np.zeros((ni, nj, nk, 3), dtype=np.float64, order="F")
-    X[..., 0] = L * u + amp * h[0] * np.sin(tp * v + 0.3) * np.cos(tp * w)
-    X[..., 1] = L * v + amp * h[1] * np.sin(tp * u + 1.1) * np.cos(tp * w + 0.2)
-    if cfg.ndim == 3:
-        X[..., 2] = L * w + amp * h[2] * np.sin(tp * u + 0.7) * np.sin(tp * v + 0.4)
-    return np.asfortranarray(X)
+    """Node coordinates of a smoothly distorted box (fiesta_gb300.grids)."""
+    from fiesta_gb300.grids import wavy_box
+    return wavy_box(cfg, amp=amp, L=L)
 
 
 class GenCase:
