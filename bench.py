@@ -426,7 +426,7 @@ def run_gen3d(n, steps, warmup, peak_gbs, peak_kind):
                          "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / nl}}
 
 
-def cpu_sample_gen3d(n_sample=96, steps=1):
+def cpu_sample_gen3d(n_sample=256, steps=1):
     """The CPU oracle's generalized 3D step on a bounded sample."""
     from oracle.oracle import Oracle
     cores = os.cpu_count() or 1
@@ -520,7 +520,8 @@ def main():
     ap.add_argument("--modes", default="plain,mixed,hybrid")
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-sample", type=int, default=128)
+    # the CPU legs run one step of the full case (seconds on a 16-core host)
+    ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-gen", action="store_true")
@@ -595,7 +596,7 @@ def main():
     if not a.no_gen:
         gen3d = run_gen3d(n, a.steps, a.warmup, peak, peak_kind)
         if not a.no_cpu:
-            gen3d["cpu_baseline"] = cpu_sample_gen3d()
+            gen3d["cpu_baseline"] = cpu_sample_gen3d(min(n, a.cpu_sample))
     cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
