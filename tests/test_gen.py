@@ -226,3 +226,22 @@ def test_gpu_deck_to_gen2d_module():
         rkAdvance(cfg, f)
     o.rk_step(3)
     assert same(f.var, o.get_state())
+
+
+@pytest.mark.gpu
+def test_gpu_gen3d_benchmark_size_matches_oracle():
+    """The generalized leg of bench.py at its full size (wavy 256^3 grid,
+    5 species): metrics and one step bit for bit with the oracle."""
+    import bench
+    cfg = bench.gen3d_cfg(256, 1.0)
+    U0, X, dt = bench.gen3d_state(cfg, 1.0)
+    cfg.dt = dt
+    o, g = Oracle(cfg), Solver(cfg)
+    for x in (o, g):
+        x.set_state(U0)
+        x.apply_bcs()
+        x.set_grid(X)
+    assert same(g.metrics(), o.metrics())
+    o.rk_step(1)
+    g.rk_step(1)
+    assert same(g.get_state(), o.get_state())
