@@ -703,7 +703,8 @@ int fst_status(fst_ctx* c, double* vmin, double* vmax, double* xmin, double* xma
 
 int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
   if (!c || !np) return FST_ERR_INVALID;
-  if (c->gen) return fail(c, FST_ERR_UNSUPPORTED, "the noise filter runs on cartesian grids");
+  if (c->gen && c->g.ndim == 3)
+    return fail(c, FST_ERR_UNSUPPORTED, "the generalized 3D module has no noise filter");
   if (np->nt < 0) return fail(c, FST_ERR_INVALID, "noise nt must be >= 0");
   const Geo& g = c->g;
   if (!c->dnoise) {  // zero-initialised like the module's FS3D_I / FS2D_I

@@ -196,11 +196,16 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
                      unsigned long long* key, const fst_noise_params& np, cudaStream_t st,
                      Prof* prof) {
   int n = 0;
-  // lattice extents (src/cart3d.cpp:326-339)
-  const int M = (g.nci + 1) % 2 == 0 ? (g.nci + 1) / 2 : g.nci / 2;
-  const int N = (g.ncj + 1) % 2 == 0 ? (g.ncj + 1) / 2 : g.ncj / 2;
+  // largest lattice index per axis (src/cart3d.cpp:326-339, src/cart2d.cpp:262-272);
+  // gen2d_func::postStep (src/gen2d.cpp:150-179) counts from nci - 1, visits
+  // one point fewer, uses no cutoff and always filters both momenta
+  const bool g2 = cf.grid_type == FST_GRID_GENERALIZED && g.ndim == 2;
+  const int M = g2 ? ((g.nci - 1) % 2 == 0 ? (g.nci - 1) / 2 : g.nci / 2) - 1
+                   : ((g.nci + 1) % 2 == 0 ? (g.nci + 1) / 2 : g.nci / 2);
+  const int N = g2 ? ((g.ncj - 1) % 2 == 0 ? (g.ncj - 1) / 2 : g.ncj / 2) - 1
+                   : ((g.ncj + 1) % 2 == 0 ? (g.ncj + 1) / 2 : g.ncj / 2);
   const int L = (g.nck + 1) % 2 == 0 ? (g.nck + 1) / 2 : g.nck / 2;
-  const bool ceq = cf.ceq != 0;
+  const bool ceq = cf.ceq != 0 && !g2;
   if (ceq) {
     const unsigned long long init = FST_KEY_LOWEST;
     cudaMemcpyAsync(key, &init, sizeof(init), cudaMemcpyHostToDevice, st);
@@ -209,7 +214,7 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
     FST_LAUNCH(prof, "noise_max", st, n, k_noise_maxabs<<<152, 256, 0, st>>>(g, U, cv, key));
   }
   int vars[3], nvars = 0;
-  if (np.mode == 1)
+  if (np.mode == 1 || g2)
     for (int d = 0; d < g.ndim; ++d) vars[nvars++] = d;
   else
     vars[nvars++] = g.ndim;
@@ -217,7 +222,9 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
   for (int q = 0; q < nvars; ++q) {
     NoiseArgs A{vars[q], M, N, L, g.nv + 1, np.dh, np.coff, cf.dx, cf.dy, dz};
     const long long cov = (long long)(2 * M + 3) * (2 * N + 3) * (g.ndim == 3 ? 2 * L + 3 : 1);
-    if (g.ndim == 3)
+    if (M < 0 || N < 0) {
+      // no lattice point (gen2d with nci or ncj <= 2): no detection
+    } else if (g.ndim == 3)
       FST_LAUNCH(prof, "noise_detect", st, n,
                  k_noise_detect<3><<<nblk(cov, 256), 256, 0, st>>>(g, U, noise, A, ceq ? key : nullptr));
     else

@@ -859,8 +859,9 @@ class Deck:
                                scheme=_SCHEMES.get(self.scheme, abi.SCHEME_WENO5))
 
     def noise_params(self):
-        """abi.FstNoiseParams of fiesta.noise, or None when the filter is off."""
-        if not self.noise:
+        """abi.FstNoiseParams of fiesta.noise, or None when the filter is off
+        (or the module has none: gen3d_func::postStep, src/gen3d.cpp:111-128)."""
+        if not self.noise or (self.grid == "generalized" and self.ndim == 3):
             return None
         return abi.FstNoiseParams(dh=self.noise_dh, eta=self.noise_eta, coff=self.noise_coff,
                                   nt=self.noise_nt, mode=self.noise_mode)
@@ -1121,8 +1122,6 @@ def _check_supported(d):
             raise DeckError("generalized grids run in the plain FP64 mode")
         if any(d.periodic[:d.ndim]):
             raise DeckError("periodic axes are not supported on generalized grids")
-        if d.noise:
-            raise DeckError("the noise filter runs on cartesian grids")
     if (d.ndim == 2 and _SCHEMES.get(d.scheme, 1) != abi.SCHEME_WENO5
             and d.mode != abi.MODE_PLAIN_FP64):
         raise DeckError(f"fiesta.advection_scheme '{d.scheme}' runs in the plain FP64 mode")

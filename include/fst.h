@@ -223,7 +223,9 @@ typedef struct fst_noise_params {
  * of a sweep in loop order (i slowest); this entry point reproduces that
  * order exactly (tile wavefronts), giving the reference's serial result bit
  * for bit.  The noise indicator persists between calls, as the module's
- * member array does.  Cartesian grids only (FST_ERR_UNSUPPORTED otherwise). */
+ * member array does.  On a generalized 2D grid it is gen2d_func's variant
+ * (src/gen2d.cpp:150-179: lattice from nci - 1, no cutoff, both momenta);
+ * the generalized 3D module has none (FST_ERR_UNSUPPORTED). */
 int fst_noise_filter(fst_ctx* ctx, const fst_noise_params* np);
 
 /* Node coordinates of a generalized grid: (ni, nj, nk, 3) doubles, LayoutLeft,

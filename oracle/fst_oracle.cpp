@@ -1114,11 +1114,19 @@ struct Oracle {
 
   void noise_filter(double n_dh, double n_eta, double n_coff, int n_nt, int n_mode) {
     if (noise.empty()) noise.assign((size_t)ngi * ngj * ngk, 0);
-    const int M = (nci + 1) % 2 == 0 ? (nci + 1) / 2 : nci / 2;
-    const int N = (ncj + 1) % 2 == 0 ? (ncj + 1) / 2 : ncj / 2;
+    // lattice points per axis: M + 1 in cart3d / cart2d (src/cart3d.cpp:326-339,
+    // src/cart2d.cpp:262-272); gen2d_func::postStep (src/gen2d.cpp:150-179)
+    // counts from nci - 1, visits M points, uses no cutoff and always
+    // filters both momenta
+    const bool g2 = gen && ndim == 2;
+    const int M = g2 ? ((nci - 1) % 2 == 0 ? (nci - 1) / 2 : nci / 2)
+                     : ((nci + 1) % 2 == 0 ? (nci + 1) / 2 : nci / 2);
+    const int N = g2 ? ((ncj - 1) % 2 == 0 ? (ncj - 1) / 2 : ncj / 2)
+                     : ((ncj + 1) % 2 == 0 ? (ncj + 1) / 2 : ncj / 2);
     const int L = (nck + 1) % 2 == 0 ? (nck + 1) / 2 : nck / 2;
+    const int Mn = g2 ? M : M + 1, Nn = g2 ? N : N + 1;
     double coff = 0.0;
-    if (cf.ceq) {
+    if (cf.ceq && !g2) {
       // 3D: maxCvar3D(var, 6), a fixed variable index; 2D: maxCvar2D(var, 1, cd)
       // = |var(nv+1)|.  Serial max from -DBL_MAX with `s > lmax`.
       const int cv = ndim == 3 ? 6 : nv + 1;
@@ -1132,7 +1140,7 @@ struct Oracle {
       coff = n_coff * mx;
     }
     std::vector<int> vars;
-    if (n_mode == 1) {
+    if (n_mode == 1 || g2) {
       for (int d = 0; d < ndim; ++d) vars.push_back(d);
     } else {
       vars.push_back(ndim);
@@ -1153,8 +1161,8 @@ struct Oracle {
                 V(i, j, k, v) += dnoise;
               }
       } else {
-        for (int ii = 0; ii < M + 1; ++ii)
-          for (int jj = 0; jj < N + 1; ++jj) detect2(ii, jj, v, n_dh, coff);
+        for (int ii = 0; ii < Mn; ++ii)
+          for (int jj = 0; jj < Nn; ++jj) detect2(ii, jj, v, n_dh, coff);
         for (int tau = 0; tau < n_nt; ++tau)
           for (int i = ng; i < ngi - ng; ++i)
             for (int j = ng; j < ngj - ng; ++j) {
@@ -1316,6 +1324,7 @@ int orc_last_max(const orc_ctx* c, double* maxS, double* maxCh) {
 }
 int orc_noise_filter(orc_ctx* c, const fst_noise_params* np) {
   if (!np) return FST_ERR_INVALID;
+  if (c->o.gen && c->o.ndim == 3) return FST_ERR_UNSUPPORTED;  // gen3d has no noise filter
   c->o.noise_filter(np->dh, np->eta, np->coff, np->nt, np->mode);
   return FST_OK;
 }

@@ -29,3 +29,14 @@ size_t ref_gen_metrics(rk_func* f, int ndim, double* out, size_t n) {
   }
   return n;
 }
+
+// gen2d_func's noise indicator (allocated by its constructor only when the
+// deck enables the filter).
+void ref_gen2d_noise_init(rk_func* f, int ngi, int ngj) {
+  auto* g = dynamic_cast<gen2d_func*>(f);
+  if (g && g->noise.size() == 0) g->noise = FS2D_I("noise", ngi, ngj);
+}
+int ref_gen2d_noise_at(rk_func* f, int i, int j) {
+  auto* g = dynamic_cast<gen2d_func*>(f);
+  return g && g->noise.size() ? g->noise(i, j) : 0;
+}

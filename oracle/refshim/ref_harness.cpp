@@ -50,6 +50,8 @@ struct ref_ctx {
 // ref_gen.cpp
 rk_func* ref_new_gen(inputConfig& cf);
 size_t ref_gen_metrics(rk_func* f, int ndim, double* out, size_t n);
+void ref_gen2d_noise_init(rk_func* f, int ngi, int ngj);
+int ref_gen2d_noise_at(rk_func* f, int i, int j);
 
 extern "C" {
 
@@ -177,13 +179,16 @@ int ref_secondary(ref_ctx* x, double* out, size_t n) {
 // order gives a defined result.
 int ref_noise_filter(ref_ctx* x, const fst_noise_params* np) {
   inputConfig& cf = x->cf;
+  if (cf.grid > 0 && cf.ndim == 3) return FST_ERR_UNSUPPORTED;  // gen3d: no noise filter
   cf.noise = true;
   cf.n_dh = np->dh;
   cf.n_eta = np->eta;
   cf.n_coff = np->coff;
   cf.n_nt = np->nt;
   cf.n_mode = np->mode;
-  if (cf.ndim == 3) {
+  if (cf.grid > 0) {  // gen2d_func::postStep (src/gen2d.cpp:150-179)
+    ref_gen2d_noise_init(x->f.get(), cf.ngi, cf.ngj);
+  } else if (cf.ndim == 3) {
     auto* f = dynamic_cast<cart3d_func*>(x->f.get());
     if (f->noise.size() == 0) f->noise = FS3D_I("noise", cf.ngi, cf.ngj, cf.ngk);
   } else {
@@ -204,7 +209,9 @@ int ref_get_noise(ref_ctx* x, int* out, size_t n) {
     for (int j = 0; j < cf.ngj; ++j)
       for (int i = 0; i < cf.ngi; ++i) {
         int v = 0;
-        if (cf.ndim == 3) {
+        if (cf.grid > 0) {
+          v = ref_gen2d_noise_at(x->f.get(), i, j);
+        } else if (cf.ndim == 3) {
           auto* f = dynamic_cast<cart3d_func*>(x->f.get());
           if (f->noise.size()) v = f->noise(i, j, k);
         } else {

@@ -61,3 +61,55 @@ def test_gpu_noise_matches_oracle(case):
         o.noise_filter(dh, 0.1, coff, nt, mode)
         s.noise_filter(dh, 0.1, coff, nt, mode)
         assert same(s.get_state(), o.get_state())
+
+
+GEN2D_CASES = [  # cells, mode, nt, dh (gen2d filters both momenta, no cutoff)
+    ((9, 8), 1, 1, 1e-3),
+    ((20, 17), 2, 2, 1e-3),
+    ((2, 6), 1, 1, 1e-3),   # no lattice point along x: removal only
+    ((31, 24), 1, 1, 5e-4),
+]
+
+
+def _gen2d_case(n, seed):
+    from tests.golden_io import wavy_nodes
+    cfg = abi.make_config(2, n, dx=(1.0, 1.0, 1.0), dt=1e-4, species=[dict(gamma=1.4, M=1.0)],
+                          R=1.0, ceq=True, grid_type=abi.GRID_GENERALIZED)
+    rng = np.random.default_rng(seed)
+    U = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, seed)
+    U = np.asfortranarray(U * (1 + 0.05 * rng.standard_normal(U.shape)))
+    return cfg, U, wavy_nodes(cfg, amp=0.2)
+
+
+@pytest.mark.skipif(not Reference.available(), reason="reference checker not built")
+@pytest.mark.parametrize("case", GEN2D_CASES)
+def test_oracle_gen2d_noise_matches_reference(case):
+    n, mode, nt, dh = case
+    cfg, U, X = _gen2d_case(n, 6)
+    o, r = Oracle(cfg), Reference(cfg)
+    for x in (o, r):
+        x.set_state(U)
+        x.set_grid(X)
+    for _ in range(2):
+        o.noise_filter(dh, 0.1, 0.5, nt, mode)
+        r.noise_filter(dh, 0.1, 0.5, nt, mode)
+        assert same(o.get_state(), r.get_state())
+        assert np.array_equal(o.noise(), r.noise())
+    if min(n) > 2:
+        assert int(o.noise().sum()) > 0 and not np.array_equal(o.get_state(), U)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", GEN2D_CASES)
+def test_gpu_gen2d_noise_matches_oracle(case):
+    from fiesta_gb300.solver import Solver
+    n, mode, nt, dh = case
+    cfg, U, X = _gen2d_case(n, 7)
+    o, s = Oracle(cfg), Solver(cfg)
+    for x in (o, s):
+        x.set_state(U)
+        x.set_grid(X)
+    for _ in range(2):
+        o.noise_filter(dh, 0.1, 0.5, nt, mode)
+        s.noise_filter(dh, 0.1, 0.5, nt, mode)
+        assert same(s.get_state(), o.get_state())
