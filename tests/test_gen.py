@@ -195,8 +195,9 @@ def test_gpu_generalized_call_order_and_limits():
     rc = lib().fst_set_grid(g._ctx, X.ctypes.data_as(C.POINTER(C.c_double)), X.size - 1)
     assert rc == abi.FST_ERR_SIZE
     g.set_grid(wavy_nodes(cfg))
+    g3 = Solver(abi.make_config(3, (4, 4, 4), dx=UNIT, dt=1e-4, R=1.0, grid_type=GEN))
     with pytest.raises(FstError):
-        g.noise_filter(1e-5, 1e-3)
+        g3.noise_filter(1e-5, 1e-3)  # gen3d_func has no noise filter
     c = Solver(abi.make_config(2, (6, 6)))
     with pytest.raises(FstError):
         c.set_grid(wavy_nodes(cfg))
