@@ -147,7 +147,7 @@ r = math.max(3, 9, 4) + math.floor(2.7) + math.sqrt(16)
     assert G["q"] == 720 and G["r"] == 9 + 2 + 4.0
 
 
-SAMPLES = "/root/reference/samples"
+SAMPLES = os.path.join(os.environ.get("FST_REFERENCE", "/root/reference"), "samples")
 
 
 @pytest.mark.skipif(not os.path.isdir(SAMPLES), reason="reference samples not present")
