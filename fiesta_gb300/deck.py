@@ -836,6 +836,9 @@ class Deck:
     noise_mode: int = 1
     scheme: str = "weno5"
     grid: str = "cartesian"
+    tdx: float = 0.0        # terrain: node spacing in x (fiesta.tdx)
+    tdy: float = 0.0        # terrain: node spacing in y (fiesta.tdy)
+    h: float = 0.0          # terrain: height of the domain top (fiesta.h)
     ng: int = 3
     mode: int = abi.MODE_PLAIN_FP64
     audit_every: int = 0
@@ -845,7 +848,7 @@ class Deck:
     def config(self):
         """The fst_config of this deck (abi.FstConfig)."""
         n = list(self.ni) + [1] * (3 - len(self.ni))
-        gen = self.grid == "generalized"
+        gen = self.grid in ("generalized", "terrain")
         # generalized grids run in computational space: dx = dy = dz = 1
         # (src/input.cpp:344-350)
         dx = [1.0, 1.0, 1.0] if gen else list(self.dx) + [self.dx[0]] * (3 - len(self.dx))
@@ -879,12 +882,21 @@ class Deck:
         except DeckError:
             raise DeckError(f"function '{name}' should return a number") from None
 
-    def grid_nodes(self, cfg=None):
+    def grid_nodes(self, cfg=None, height=None):
         """Node coordinates of a generalized grid, (ni, nj, nk, 3) with
         ni = nci + 1: ``fiesta.initialize_grid(i, j, k, v)`` for v < ndim at
-        every node, as loadGrid (src/input.cpp:529-560) on one rank."""
+        every node, as loadGrid (src/input.cpp:529-560) on one rank.  A
+        terrain grid is built from the ground heights ``height`` (ni, nj),
+        which the reference reads from its restart file's "Height" dataset
+        (HDF5, not readable here), and fiesta.tdx / tdy / h."""
         import numpy as np
         cfg = cfg or self.config()
+        if self.grid == "terrain":
+            from .grids import terrain_nodes
+            if height is None:
+                raise DeckError("a terrain grid needs the ground heights (the 'Height' dataset "
+                                "of the restart file): pass height=")
+            return terrain_nodes(cfg, height, self.tdx, self.tdy, self.h)
         ni, nj, nk, _ = abi.grid_dims(cfg)
         X = np.zeros((ni, nj, nk, 3), order="F")
         for v in range(cfg.ndim):
@@ -1046,6 +1058,10 @@ def load(path=None, text=None):
     d.scheme = rd.get(["advection_scheme"], str, "weno5")
     d.grid = rd.get(["grid", "type"], str, "cartesian")
     d.dx = rd.array(["grid", "dx"], d.ndim, float)
+    if d.grid == "terrain" and d.ndim == 3:  # src/input.cpp:294-302
+        d.tdx = rd.get(["tdx"], float)
+        d.tdy = rd.get(["tdy"], float)
+        d.h = rd.get(["h"], float)
     d.ni = rd.array(["grid", "ni"], d.ndim, "size")
     d.procs = rd.array(["mpi", "procs"], d.ndim, "size")
     bcs = [abi.BC_OUTFLOW] * 6
@@ -1112,12 +1128,11 @@ def _check_supported(d):
     """What the library's right-hand side covers: cartesian and generalized
     grids; the three 2D advection schemes (an unknown scheme name leaves
     WENO5, as src/input.cpp:317-323 does); the 3D modules use WENO5."""
-    if d.grid == "terrain":
-        raise DeckError("fiesta.grid.type 'terrain' is not supported (it reads a terrain "
-                        "file through the HDF5 writer)")
-    if d.grid not in ("cartesian", "generalized"):
+    if d.grid == "terrain" and d.ndim != 3:
+        raise DeckError("ndim must be equal to 3 for terrain")  # src/input.cpp:303-305
+    if d.grid not in ("cartesian", "generalized", "terrain"):
         raise DeckError(f"unknown fiesta.grid.type '{d.grid}'")
-    if d.grid == "generalized":
+    if d.grid in ("generalized", "terrain"):
         if d.mode != abi.MODE_PLAIN_FP64:
             raise DeckError("generalized grids run in the plain FP64 mode")
         if any(d.periodic[:d.ndim]):

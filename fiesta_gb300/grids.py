@@ -25,3 +25,26 @@ def wavy_box(cfg, amp=0.2, L=1.0):
     if cfg.ndim == 3:
         X[..., 2] = L * w + amp * h[2] * np.sin(tp * u + 0.7) * np.sin(tp * v + 0.4)
     return np.asfortranarray(X)
+
+
+def terrain_nodes(cfg, height, tdx, tdy, top):
+    """Nodes of a terrain-following grid (fiesta.grid.type = "terrain"), as
+    readTerrain builds them (src/reader.cpp:121-160): x = tdx*i, y = tdy*j and
+    z = h + dz*k with dz = (top - h)/nck, for the ground height h(i, j) given
+    at the (nci+1) x (ncj+1) nodes (the restart file's "Height" dataset).
+    `tdx`, `tdy`, `top` are the deck's fiesta.tdx, fiesta.tdy, fiesta.h."""
+    if cfg.ndim != 3:
+        raise ValueError("terrain grids are 3D")
+    ni, nj, nk = cfg.nci + 1, cfg.ncj + 1, cfg.nck + 1
+    h = np.asarray(height, dtype=np.float64)
+    if h.shape != (ni, nj):
+        raise ValueError(f"height shape {h.shape} != {(ni, nj)}")
+    X = np.zeros((ni, nj, nk, 3), dtype=np.float64, order="F")
+    i = np.arange(ni, dtype=np.float64)[:, None, None]
+    j = np.arange(nj, dtype=np.float64)[None, :, None]
+    k = np.arange(nk, dtype=np.float64)[None, None, :]
+    X[..., 0] = tdx * i
+    X[..., 1] = tdy * j
+    dz = (top - h) / cfg.nck
+    X[..., 2] = h[:, :, None] + dz[:, :, None] * k
+    return np.asfortranarray(X)

@@ -109,8 +109,8 @@ def test_required_keys_and_errors():
         deck.load(text=DECK_3D.replace('"reflective"', '"wall"'))
     with pytest.raises(deck.DeckError, match="fiesta.bc.xmin"):
         deck.load(text=DECK_3D.replace("fiesta.bc.xperiodic = true", ""))
-    with pytest.raises(deck.DeckError, match="not supported"):
-        deck.load(text=DECK_3D.replace('"cartesian"', '"terrain"'))
+    with pytest.raises(deck.DeckError, match="unknown fiesta.grid.type"):
+        deck.load(text=DECK_3D.replace('"cartesian"', '"curvy"'))
     with pytest.raises(deck.DeckError, match="periodic"):
         deck.load(text=DECK_3D.replace('"cartesian"', '"generalized"')
                   .replace('mode = "mixed"', 'mode = "plain"'))
@@ -218,3 +218,50 @@ def test_generalized_deck_grid_and_cell_centres():
     bad = DECK_GEN2D.replace("return 0\nend", "end")
     with pytest.raises(deck.DeckError, match="should return a number"):
         deck.load(text=bad).initial_conditions(cfg, X)
+
+
+DECK_TERRAIN = """
+fiesta.title = "valley"
+fiesta.species = {{name="air", gamma=1.4, M=0.02897, mu=1.8e-5}}
+fiesta.time.dt = 1e-4
+fiesta.grid.type = "terrain"
+fiesta.grid.ndim = 3
+fiesta.grid.ni = {6, 5, 4}
+fiesta.grid.dx = {1, 1, 1}
+fiesta.tdx = 10.0
+fiesta.tdy = 12.5
+fiesta.h = 100.0
+fiesta.bc.xmin = "outflow"
+fiesta.bc.xmax = "outflow"
+fiesta.bc.ymin = "outflow"
+fiesta.bc.ymax = "outflow"
+fiesta.bc.zmin = "reflective"
+fiesta.bc.zmax = "outflow"
+fiesta.mpi.procs = {1, 1, 1}
+function fiesta.initial_conditions(x, y, z, v)
+    if v == 3 then return 2.5e5 end
+    if v == 4 then return 1.2 end
+    return 0
+end
+"""
+
+
+def test_terrain_deck_and_nodes():
+    d = deck.load(text=DECK_TERRAIN)
+    cfg = d.config()
+    assert cfg.grid_type == abi.GRID_GENERALIZED and (cfg.dx, cfg.dy, cfg.dz) == (1.0, 1.0, 1.0)
+    assert (d.tdx, d.tdy, d.h) == (10.0, 12.5, 100.0)
+    with pytest.raises(deck.DeckError, match="ground heights"):
+        d.grid_nodes(cfg)
+    hgt = np.fromfunction(lambda i, j: 3.0 * i + 0.5 * j * j, (7, 6))
+    X = d.grid_nodes(cfg, height=hgt)
+    i, j, k = 5, 4, 3
+    assert X[i, j, k, 0] == 10.0 * i and X[i, j, k, 1] == 12.5 * j
+    assert X[i, j, k, 2] == hgt[i, j] + (100.0 - hgt[i, j]) / 4 * k
+    U = d.initial_conditions(cfg, X)
+    assert U[3, 3, 3, 3] == 2.5e5 and np.all(U[..., 0] == 0)
+    with pytest.raises(deck.DeckError, match="fiesta.tdx"):
+        deck.load(text=DECK_TERRAIN.replace("fiesta.tdx = 10.0", ""))
+    with pytest.raises(deck.DeckError, match="ndim must be equal to 3"):
+        deck.load(text=DECK_TERRAIN.replace("fiesta.grid.ndim = 3", "fiesta.grid.ndim = 2")
+                  .replace("{6, 5, 4}", "{6, 5}"))
