@@ -1146,3 +1146,40 @@ def _check_supported(d):
         raise DeckError("fiesta.species is empty")
     if len(d.species) > abi.FST_MAX_SPECIES:
         raise DeckError(f"at most {abi.FST_MAX_SPECIES} species")
+
+
+def export(path, prefix, height=None):
+    """Write what a C++ host needs to start a run of the deck at ``path``:
+    ``<prefix>.cfg`` (the raw fst_config, read by fst::load_config in
+    include/fst_module.hpp), ``<prefix>.U0`` (the initial state, LayoutLeft
+    FP64), ``<prefix>.X`` (generalized and terrain grids: the node
+    coordinates) and ``<prefix>.json`` (a readable summary)."""
+    import ctypes as C
+    import json
+
+    import numpy as np
+    d = load(path)
+    cfg = d.config()
+    X = None
+    if cfg.grid_type == abi.GRID_GENERALIZED:
+        X = d.grid_nodes(cfg, height=height)
+    U0 = d.initial_conditions(cfg, X)
+    with open(prefix + ".cfg", "wb") as f:
+        f.write(bytes(C.string_at(C.addressof(cfg), C.sizeof(cfg))))
+    np.asfortranarray(U0).ravel(order="F").astype("<f8").tofile(prefix + ".U0")
+    if X is not None:
+        np.asfortranarray(X).ravel(order="F").astype("<f8").tofile(prefix + ".X")
+    summary = {"deck": path, "title": d.title, "nt": d.nt, "dt": d.dt,
+               "state_shape": list(abi.dims(cfg)), "grid": d.grid,
+               "grid_shape": list(abi.grid_dims(cfg)) if X is not None else None,
+               "noise": d.noise_params() is not None, "config": abi.config_to_dict(cfg)}
+    with open(prefix + ".json", "w") as f:
+        json.dump(summary, f, indent=1)
+    return summary
+
+
+if __name__ == "__main__":
+    import sys
+    if len(sys.argv) != 3:
+        sys.exit("usage: python -m fiesta_gb300.deck <deck.lua> <output prefix>")
+    print(export(sys.argv[1], sys.argv[2])["state_shape"])

@@ -18,6 +18,7 @@
 #define FST_MODULE_HPP
 
 #include <cstddef>
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -157,6 +158,31 @@ class gen2d_func : public gen_func {
     if (cf.ndim != 2) throw Error(FST_ERR_INVALID, "gen2d_func needs ndim = 2");
   }
 };
+
+// A config written by `python -m fiesta_gb300.deck <deck.lua> <prefix>`
+// (<prefix>.cfg, the raw struct): the deck's keys, read by the library's
+// Lua-subset reader, for a C++ host.
+inline fst_config load_config(const std::string& path) {
+  fst_config c;
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) throw Error(FST_ERR_INVALID, "cannot open " + path);
+  const size_t got = std::fread(&c, 1, sizeof(c), f);
+  const bool more = std::fgetc(f) != EOF;
+  std::fclose(f);
+  if (got != sizeof(c) || more) throw Error(FST_ERR_SIZE, path + " is not an fst_config");
+  if (c.abi_version != FST_ABI_VERSION) throw Error(FST_ERR_INVALID, path + ": ABI version");
+  return c;
+}
+
+// Raw FP64 array (<prefix>.U0, <prefix>.X) into a host mirror of its size.
+inline void load_array(const std::string& path, HostArray& a) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) throw Error(FST_ERR_INVALID, "cannot open " + path);
+  const size_t got = std::fread(a.data(), sizeof(double), a.size(), f);
+  const bool more = std::fgetc(f) != EOF;
+  std::fclose(f);
+  if (got != a.size() || more) throw Error(FST_ERR_SIZE, path + ": size does not match");
+}
 
 // The module src/main.cpp:40-50 picks for a config.
 inline std::unique_ptr<rk_func> make_module(const fst_config& cf) {

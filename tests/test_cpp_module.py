@@ -32,7 +32,7 @@ def _compile(name, outdir):
     return exe
 
 
-@pytest.mark.parametrize("name", ["module_bc", "module_step"])
+@pytest.mark.parametrize("name", ["module_bc", "module_step", "module_deck"])
 def test_cpp_module_programs_compile_and_link(name, tmp_path):
     assert os.path.exists(_compile(name, str(tmp_path)))
 
@@ -72,3 +72,46 @@ def test_gpu_cpp_module_steps_match_oracle(tmp_path):
     o.set_grid(arr("X", abi.grid_dims(cfg)))
     o.rk_step(3)
     assert same(arr("U1", shape), o.get_state())
+
+
+def test_deck_export_round_trip(tmp_path):
+    """The exported config, state and grid read back as written."""
+    from fiesta_gb300 import deck
+    from tests.test_deck import DECK_GEN2D
+    p = tmp_path / "wavy.lua"
+    p.write_text(DECK_GEN2D)
+    summary = deck.export(str(p), str(tmp_path / "wavy"))
+    cfg = abi.FstConfig.from_buffer_copy(open(tmp_path / "wavy.cfg", "rb").read())
+    d = deck.load(str(p))
+    assert bytes(cfg) == bytes(d.config())
+    X = np.fromfile(tmp_path / "wavy.X", dtype="<f8").reshape(abi.grid_dims(cfg), order="F")
+    assert np.array_equal(X, d.grid_nodes(cfg))
+    assert summary["state_shape"] == list(abi.dims(cfg))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["cart3d", "gen2d"])
+def test_gpu_cpp_runs_an_exported_deck(which, tmp_path):
+    """deck.lua -> python -m fiesta_gb300.deck -> C++ module interface ->
+    the same state as the oracle on the same inputs."""
+    from tests.test_deck import DECK_3D, DECK_GEN2D
+    text = DECK_3D.replace('mode = "mixed"', 'mode = "plain"') if which == "cart3d" else DECK_GEN2D
+    p = tmp_path / "deck.lua"
+    p.write_text(text)
+    prefix = str(tmp_path / "run")
+    r = subprocess.run(["python", "-m", "fiesta_gb300.deck", str(p), prefix], cwd=ROOT,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([_compile("module_deck", str(tmp_path)), prefix, "2"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    cfg = abi.FstConfig.from_buffer_copy(open(prefix + ".cfg", "rb").read())
+    shape = abi.dims(cfg)
+    U0 = np.fromfile(prefix + ".U0", dtype="<f8").reshape(shape, order="F")
+    U1 = np.fromfile(prefix + ".U1", dtype="<f8").reshape(shape, order="F")
+    o = Oracle(cfg)
+    o.set_state(U0)
+    if cfg.grid_type == abi.GRID_GENERALIZED:
+        o.set_grid(np.fromfile(prefix + ".X", dtype="<f8").reshape(abi.grid_dims(cfg), order="F"))
+    o.rk_step(2)
+    assert same(U1, o.get_state())
