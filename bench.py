@@ -184,6 +184,10 @@ def algorithmic_bytes(kernel, cfg):
     if getattr(cfg, "grid_type", 0) == 1:
         tab["prim3d"] = 8 * allc * (nv + 9 + 5)
         tab["cell3d"] = 8 * inner * (3 * nv + 1 + 9 + 2 * nvt)
+        # mixed: the pressure pair and 18 FP32 metric fields in, the momenta,
+        # energy and C-variables old and new
+        tab["gen_cell"] = inner * (4 * (2 + 18) + 16 * (4 + (nvt - nv)))
+        tab["gen_tvel"] = allc * 4 * (3 + 9 + 3)
     tab["mspec3d_hybrid"] = tab["mspec3d"] + inner * 3
     tab["mmom3d_hybrid"] = tab["mmom3d"] + inner * 3
     return tab.get(kernel)
@@ -359,10 +363,10 @@ def run_batch2d(steps, warmup, ncases=64):
                         "C-equation, buoyancy; mixed precision; CUDA graph per step"}
 
 
-def gen3d_cfg(n, dt):
+def gen3d_cfg(n, dt, mode=0):
     from fiesta_gb300 import abi
     return abi.make_config(3, (n, n, n), dx=(1.0, 1.0, 1.0), dt=dt, species=SPECIES,
-                           grid_type=abi.GRID_GENERALIZED)
+                           grid_type=abi.GRID_GENERALIZED, mode=mode)
 
 
 def gen3d_state(cfg, L):
@@ -378,13 +382,13 @@ def gen3d_state(cfg, L):
     return U0, X, 0.4 / S
 
 
-def run_gen3d(n, steps, warmup, peak_gbs, peak_kind):
+def run_gen3d(n, steps, warmup, peak_gbs, peak_kind, mode=0):
     """The generalized-grid module (gen3d_func::compute) on a wavy 1 m box,
-    plain FP64: Mcell-steps/s, the dominant kernel's roofline, and the CPU
-    oracle on a bounded sample of the same case."""
+    plain FP64 (mode 0) or mixed (mode 1): Mcell-steps/s and the dominant
+    kernel's roofline; returns the final state as well."""
     import torch
     from fiesta_gb300.solver import Solver
-    cfg = gen3d_cfg(n, 1.0)
+    cfg = gen3d_cfg(n, 1.0, mode)
     U0, X, dt = gen3d_state(cfg, 1.0)
     cfg.dt = dt
     s = Solver(cfg)
@@ -410,20 +414,23 @@ def run_gen3d(n, steps, warmup, peak_gbs, peak_kind):
     s.set_profiling(False)
     launches = s.stats()["kernel_launches"] - l0
     finite = s.check_finite()
+    U = s.get_state()
     s.close()
     top = max(kt.items(), key=lambda kv: kv[1][1])
     name, (nl, tot) = top
     b = algorithmic_bytes(name, cfg)
-    ach = b / (tot / nl / 1e3) / 1e9
-    return {"value": n ** 3 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-steps/s",
-            "ms_per_step": ms / steps, "gpu_launches": launches, "finite": finite,
-            "dtype": "f64",
-            "workload": f"gen3d_func::compute on a wavy {n}^3 grid, 5 species, "
-                        "plain FP64 (bit-identical to the reference)",
-            "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
-            "roofline": {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak_gbs,
-                         "unit": "GB/s", "frac": ach / peak_gbs, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / nl}}
+    ach = b / (tot / nl / 1e3) / 1e9 if b else None
+    form = ("plain FP64 (bit-identical to the reference)" if mode == 0
+            else "mixed precision (FP32 fluxes, FP64 state and pressure recovery)")
+    return U, {"value": n ** 3 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-steps/s",
+               "ms_per_step": ms / steps, "gpu_launches": launches, "finite": finite,
+               "dtype": "f64" if mode == 0 else "f32+f64",
+               "workload": f"gen3d_func::compute on a wavy {n}^3 grid, 5 species, {form}",
+               "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
+               "roofline": {"bound": "fp64" if mode == 0 else "hbm", "kernel": name,
+                            "achieved_hbm_gbs": ach, "peak_hbm_gbs": peak_gbs,
+                            "hbm_frac": ach / peak_gbs if ach else None, "peak_source": peak_kind,
+                            "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / nl}}
 
 
 def cpu_sample_gen3d(n_sample=256, steps=1):
@@ -594,7 +601,20 @@ def main():
     batch = None if a.no_batch else run_batch2d(a.steps, a.warmup)
     gen3d = None
     if not a.no_gen:
-        gen3d = run_gen3d(n, a.steps, a.warmup, peak, peak_kind)
+        Up, gen3d = run_gen3d(n, a.steps, a.warmup, peak, peak_kind, 0)
+        Um, gen3d["mixed"] = run_gen3d(n, a.steps, a.warmup, peak, peak_kind, 1)
+        gcfg = gen3d_cfg(n, 1.0)
+        ng, nsteps = gcfg.ng, a.warmup + a.steps
+        U0, _, _ = gen3d_state(gcfg, 1.0)
+        rows = {}
+        for v in range(Up.shape[3]):  # momenta by their increments (they start at zero)
+            z = U0[ng:-ng, ng:-ng, ng:-ng, v] if v < 3 else 0.0
+            pa, ma = Up[ng:-ng, ng:-ng, ng:-ng, v] - z, Um[ng:-ng, ng:-ng, ng:-ng, v] - z
+            nb = np.linalg.norm(pa.ravel())
+            rows[v] = float(np.linalg.norm((ma - pa).ravel()) / nb) if nb > 0 else 0.0
+        gen3d["mixed"]["rel_l2_vs_plain_after_steps"] = {"steps": nsteps, "max": max(rows.values()),
+                                                          "per_variable": rows}
+        del Up, Um
         if not a.no_cpu:
             gen3d["cpu_baseline"] = cpu_sample_gen3d(min(n, a.cpu_sample))
     cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)

@@ -6,6 +6,7 @@ Translation units and their floating-point contract:
       reproduces the reference's FP64 arithmetic operation for operation
   fst_mixed.cu, fst_mixed3d.cu, fst_hybrid.cu, fst_batch.cu
                                               FMA on, fast FP32 math
+  fst_mixedgen.cu                             IEEE FP32 (pair arithmetic)
   fst_api.cu                                  host orchestration
   fst_host.cpp                                host IC generator, g++ with
       -ffp-contract=off so the same seed gives the same bits on x86 and Arm
@@ -37,6 +38,7 @@ UNITS = [
     ("fst_noalloc.cu", ["--fmad=false"]),
     ("fst_noise.cu", ["--fmad=false"]),
     ("fst_gen.cu", ["--fmad=false"]),
+    ("fst_mixedgen.cu", []),
 ]
 HOST_UNITS = ["fst_host.cpp"]
 

@@ -109,7 +109,8 @@ std::string validate(const fst_config* cf) {
   if (cf->ndim == 2 && cf->scheme > FST_SCHEME_WENO5 && cf->mode != FST_MODE_PLAIN_FP64)
     return "the centered4 and quick schemes run in FST_MODE_PLAIN_FP64";
   if (cf->grid_type == FST_GRID_GENERALIZED) {
-    if (cf->mode != FST_MODE_PLAIN_FP64) return "generalized grids run in FST_MODE_PLAIN_FP64";
+    if (cf->mode == FST_MODE_HYBRID || (cf->mode == FST_MODE_MIXED && cf->ndim != 3))
+      return "generalized grids run in FST_MODE_PLAIN_FP64 (and FST_MODE_MIXED in 3D)";
     // the reference's gen2d / gen3d modules exchange no halo and apply no
     // boundary conditions, so a periodic axis has no meaning there
     if (cf->xper || cf->yper || (cf->ndim == 3 && cf->zper))
@@ -149,7 +150,9 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
   }
   P.dx = cf.dx;
   P.dy = cf.dy;
-  P.dz = g.ndim == 3 ? cf.dz : cf.dx;  // 2D: dz = dx (src/input.cpp:402)
+  // 2D: dz = dx (src/input.cpp:402); the generalized 3D module passes cf.dx as
+  // the z spacing of its fluxes (src/gen3d.cpp:359), its only use of dz
+  P.dz = g.ndim == 3 && cart ? cf.dz : cf.dx;
   P.ddx = make_div(P.dx);
   P.ddy = make_div(P.dy);
   P.ddz = make_div(P.dz);
@@ -177,7 +180,6 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
     P.dxmag2 = P.dx * P.dx + P.dy * P.dy;
     P.dxmag = std::sqrt(P.dx * P.dx + P.dy * P.dy);
   }
-  if (!cart && g.ndim == 3) P.ddz = make_div(P.dx);  // calculateFluxesG(..., cf.dx, cf.dy, cf.dx, v)
   P.mu2d = 2.928e-5;
   P.kheat2d = 0.026;
   P.rd_f[0] = (float)(1.0 / P.dx);
@@ -590,10 +592,13 @@ int fst_set_grid(fst_ctx* c, const double* nodes, size_t n) {
     cudaGetLastError();
     return fail(c, FST_ERR_OOM, "grid buffer allocation failed");
   }
-  double* met = c->g.ndim == 3 ? c->b3.met : c->b2.met;
+  const bool mixed = c->cf.mode != FST_MODE_PLAIN_FP64;
+  double* met = mixed ? c->bm.met64 : c->g.ndim == 3 ? c->b3.met : c->b2.met;
   e = cudaMemcpyAsync(dX, nodes, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
     c->stats.kernel_launches += fst_gen_metrics(c->g, dX, met, c->stream);
+    if (mixed)
+      c->stats.kernel_launches += fst_mixedgen_pair(c->g, c->bm.gq, met, c->bm.metf, c->stream);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -607,7 +612,9 @@ int fst_get_metrics(fst_ctx* c, double* out, size_t n) {
   if (!c || !out) return FST_ERR_INVALID;
   if (!c->gen) return fail(c, FST_ERR_UNSUPPORTED, "not a generalized-grid context");
   if (n != fst_metrics_size(&c->cf)) return fail(c, FST_ERR_SIZE, "metrics size mismatch");
-  const double* met = c->g.ndim == 3 ? c->b3.met : c->b2.met;
+  const double* met = c->cf.mode != FST_MODE_PLAIN_FP64 ? c->bm.met64
+                     : c->g.ndim == 3                     ? c->b3.met
+                                                          : c->b2.met;
   cudaError_t e = cudaMemcpyAsync(out, met, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "get_metrics");

@@ -62,6 +62,16 @@ std::string fst_setup_geo_phys(const fst_config* cfg, Geo& g, Phys& P);
 // fst_gen.cu: metric tensor of a generalized grid from its node coordinates
 int fst_gen_metrics(const Geo& g, const double* nodes, double* met, cudaStream_t st);
 
+struct MixedView;
+// fst_mixedgen.cu: the mixed path's generalized-grid pieces
+int fst_mixedgen_pair(const Geo& g, const Geo& gq, const double* met, float* metf,
+                      cudaStream_t st);
+int fst_mixedgen_tvel(const Geo& g, const Geo& gq, const float* metf, float* vel,
+                      cudaStream_t st);
+int fst_mixedgen_cell(const Geo& g, const Geo& gq, const MixedView& M, const float* metf,
+                      const double* Uold, double* Unew, double coef, double* Rout,
+                      cudaStream_t st);
+
 // fst_bc.cu
 int fst_launch_bcs(const Geo& g, const fst_config& cf, double* U, cudaStream_t stream, Prof* prof);
 
@@ -125,6 +135,10 @@ struct MixedBufs {
   // and the device error word (FST_DEVERR_* bits; a TMA wait that ran out)
   Mixed3DMaps* maps3d;
   unsigned int* dev_err;
+  // generalized 3D grids: the FP64 metric tensor (state layout, 9 fields)
+  // and its FP32 pairs hi [9] + lo [9] in the primitives' layout
+  double* met64;
+  float* metf;
 };
 struct MixedView {
   const float* Q;    // [nv][cells] conserved variables, Q[ndim] = E + p

@@ -126,8 +126,9 @@ size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g) {
   // floats: Q nv, rho, vel ndim, mu, nrg, C 5, T; doubles: p, rho and the
   // FP64 secondary outputs (rho, p, vel, T); hybrid: 3 map bytes
   const size_t fl = g.nv + 1 + g.ndim + 1 + 1 + 5 + 1 + 2;
-  (void)cf;
-  return (fl + 1) / 2 + 1 + (size_t)(g.ndim + 3) + 1;
+  // generalized grids: 9 FP64 metrics + 18 FP32 metric pairs
+  const size_t gen = cf.grid_type == FST_GRID_GENERALIZED ? 9 + 9 : 0;
+  return (fl + 1) / 2 + 1 + (size_t)(g.ndim + 3) + 1 + gen;
 }
 
 int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc,
@@ -158,6 +159,10 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   A((void**)&b.red, sizeof(unsigned long long) * 2);
   A((void**)&b.counters, sizeof(unsigned long long) * 8);
   A((void**)&b.dev_err, sizeof(unsigned int));
+  if (cf.grid_type == FST_GRID_GENERALIZED) {
+    A((void**)&b.met64, sizeof(double) * ns * 9);
+    A((void**)&b.metf, sizeof(float) * n * 18);
+  }
   if (!rc && cf.mode == FST_MODE_HYBRID) rc = fst_hybrid_alloc(cf, g, b, alloc);
   if (!rc) rc = fst_mixed3d_prepare(g, b, why);
   return rc;
@@ -177,6 +182,8 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
                launch_mprim<3>(g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
                                P.visc ? b.mu32 : nullptr, P.ceq ? b.nrg : nullptr,
                                P.ceq ? b.C : nullptr, nullptr, P.ceq ? b.red : nullptr, st));
+    if (b.metf)  // generalized grid: contravariant velocity for the face kernels
+      FST_LAUNCH(prof, "gen_tvel", st, n, fst_mixedgen_tvel(g, b.gq, b.metf, b.vel32, st));
   } else {
     FST_LAUNCH(prof, "mprim2d", st, n,
                launch_mprim<2>(g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,

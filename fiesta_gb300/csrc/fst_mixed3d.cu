@@ -1033,7 +1033,12 @@ int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const Mixed
                     double* Rout, cudaStream_t st, Prof* prof, bool hybrid) {
   int n = 0;
   // cell terms first: k_mmom3d adds its face terms to what k_mcell3d wrote
-  FST_LAUNCH(prof, "mcell3d", st, n, launch_cell(g, P, b, M, Uold, Unew, coef, Rout, st));
+  // (on a generalized grid, the metric pressure gradient)
+  if (b.metf)
+    FST_LAUNCH(prof, "gen_cell", st, n,
+               fst_mixedgen_cell(g, b.gq, M, b.metf, Uold, Unew, coef, Rout, st));
+  else
+    FST_LAUNCH(prof, "mcell3d", st, n, launch_cell(g, P, b, M, Uold, Unew, coef, Rout, st));
   if (hybrid) {
     FST_LAUNCH(prof, "mspec3d_hybrid", st, n,
                n += launch_spec_any<true>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st) - 1);

@@ -1133,8 +1133,8 @@ def _check_supported(d):
     if d.grid not in ("cartesian", "generalized", "terrain"):
         raise DeckError(f"unknown fiesta.grid.type '{d.grid}'")
     if d.grid in ("generalized", "terrain"):
-        if d.mode != abi.MODE_PLAIN_FP64:
-            raise DeckError("generalized grids run in the plain FP64 mode")
+        if d.mode == abi.MODE_HYBRID or (d.mode == abi.MODE_MIXED and d.ndim != 3):
+            raise DeckError("generalized grids run in the plain FP64 mode (and mixed in 3D)")
         if any(d.periodic[:d.ndim]):
             raise DeckError("periodic axes are not supported on generalized grids")
     if (d.ndim == 2 and _SCHEMES.get(d.scheme, 1) != abi.SCHEME_WENO5

@@ -73,7 +73,8 @@ enum {
 
 /* Grid type (fiesta.grid.type, src/input.cpp:287-350).  GENERALIZED runs the
  * reference's gen2d / gen3d modules (src/gen2d.cpp, src/gen3d.cpp): curvilinear
- * node coordinates given by fst_set_grid, metric terms on every cell. */
+ * node coordinates given by fst_set_grid, metric terms on every cell; plain
+ * FP64 (2D and 3D) or, in 3D, FST_MODE_MIXED. */
 enum {
   FST_GRID_CARTESIAN = 0,
   FST_GRID_GENERALIZED = 1

@@ -115,7 +115,8 @@ def test_required_keys_and_errors():
         deck.load(text=DECK_3D.replace('"cartesian"', '"generalized"')
                   .replace('mode = "mixed"', 'mode = "plain"'))
     with pytest.raises(deck.DeckError, match="plain FP64"):
-        deck.load(text=DECK_3D.replace('"cartesian"', '"generalized"'))
+        deck.load(text=DECK_3D.replace('"cartesian"', '"generalized"')
+                  .replace('mode = "mixed"', 'mode = "hybrid"'))
     d = deck.load(text=DECK_3D.replace('"weno5"', '"centered4"'))
     assert d.config().scheme == abi.SCHEME_CENTERED4  # the 3D modules ignore it
     d = deck.load(text=DECK_3D.replace('"weno5"', '"upwind"'))

@@ -106,7 +106,8 @@ def test_config_checks_without_gpu():
     L = lib()
     base = dict(dx=UNIT, dt=1e-4, R=1.0, grid_type=GEN)
     bad = [abi.make_config(3, (4, 4, 4), periodic=(False, True, False), **base),
-           abi.make_config(3, (4, 4, 4), mode=abi.MODE_MIXED, **base),
+           abi.make_config(3, (4, 4, 4), mode=abi.MODE_HYBRID, **base),
+           abi.make_config(2, (4, 4), mode=abi.MODE_MIXED, **base),
            abi.make_config(2, (4, 4), mode=abi.MODE_MIXED, scheme="quick", dx=UNIT),
            abi.make_config(2, (4, 4), scheme=7, dx=UNIT)]
     for cfg in bad:
@@ -268,3 +269,41 @@ def test_gpu_terrain_grid_matches_oracle():
     o.rk_step(2)
     g.rk_step(2)
     assert same(g.get_state(), o.get_state())
+
+
+def _rel(a, b):
+    d = np.linalg.norm((a - b).ravel())
+    n = np.linalg.norm(b.ravel())
+    return d / n if n > 0 else d
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,ceq", [((24, 20, 18), False), ((40, 33, 29), True)])
+def test_gpu_mixed_generalized_within_1e5_of_fp64(n, ceq):
+    """The mixed-precision form of the generalized 3D module against its FP64
+    form (bit-identical to the reference): every conserved field within
+    rel-L2 1e-5 after a few steps (momenta by their increments)."""
+    sp = [dict(gamma=1.4, M=0.02896), dict(gamma=1.67, M=0.004)]
+    cfg = abi.make_config(3, n, dx=UNIT, dt=1.0, species=sp, grid_type=GEN, ceq=ceq)
+    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 4, p_ambient=1e5, T_ambient=300.0,
+                            nkernels=3)
+    X = wavy_nodes(cfg, amp=0.25)
+    import bench
+    S = bench.max_wave_speed(cfg, U0) * n[0]  # cells per second on the unit box
+    cfg.dt = 0.4 / S
+    mcfg = abi.config_from_dict(abi.config_to_dict(cfg))
+    mcfg.mode = abi.MODE_MIXED
+    p, m = Solver(cfg), Solver(mcfg)
+    for x in (p, m):
+        x.set_state(U0)
+        x.apply_bcs()
+        x.set_grid(X)
+    assert same(m.metrics(), p.metrics())
+    p.rk_step(4)
+    m.rk_step(4)
+    Up, Um = p.get_state(), m.get_state()
+    ng = cfg.ng
+    for v in range(abi.dims(cfg)[3]):
+        a = Um[ng:-ng, ng:-ng, ng:-ng, v] - (U0[ng:-ng, ng:-ng, ng:-ng, v] if v < 3 else 0)
+        b = Up[ng:-ng, ng:-ng, ng:-ng, v] - (U0[ng:-ng, ng:-ng, ng:-ng, v] if v < 3 else 0)
+        assert _rel(a, b) <= 1e-5, (v, _rel(a, b))
