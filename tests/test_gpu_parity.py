@@ -134,3 +134,42 @@ def test_gpu_degenerate_periodic(n):
     o.rk_step(2)
     g.rk_step(2)
     assert same(g.get_state(), o.get_state())
+
+
+def test_gpu_mixed_beyond_32bit_state_indices():
+    """530^3 interior, 5 species, C-equation: the state holds 536^3 x 14 =
+    2.16e9 doubles, past 2^31, so every variable offset of the last fields
+    needs 64-bit indexing.  One mixed-precision step with periodic
+    boundaries: finite, species masses conserved to round-off, and the last
+    C-variable of the last interior cell updated."""
+    cfg = mixing_config((530, 530, 530))
+    cfg.mode = abi.MODE_MIXED
+    cfg.xper = cfg.yper = cfg.zper = 1
+    ngi, ngj, ngk, nvt = abi.dims(cfg)
+    assert ngi * ngj * ngk * nvt > 2 ** 31
+    ng = cfg.ng
+    # a smooth periodic state built by broadcasting (fast at this size)
+    tp = 2.0 * np.pi
+    x = (np.arange(ngi) - ng + 0.5) / 530
+    sx = np.sin(tp * x)[:, None, None]
+    cy = np.cos(tp * x)[None, :, None]
+    sz = np.sin(tp * x)[None, None, :]
+    U0 = np.zeros((ngi, ngj, ngk, nvt), order="F")
+    rho = 0.0
+    for s_ in range(5):
+        U0[..., 4 + s_] = 0.2 * (1.0 + 0.05 * (s_ + 1) * sx * cy)
+        rho = rho + U0[..., 4 + s_]
+    U0[..., 0] = 10.0 * sz * rho
+    U0[..., 3] = 2.5e5 * (1.0 + 0.01 * cy * sz)
+    U0[..., nvt - 1] = 0.1  # a C-variable the step must move
+    g = Solver(cfg)
+    g.set_state(U0)
+    g.rk_step(1)
+    assert g.check_finite()
+    U = g.get_state()
+    last = (ngi - ng - 1, ngj - ng - 1, ngk - ng - 1, nvt - 1)
+    assert U[last] != U0[last]
+    for s in range(5):
+        m0 = interior(cfg, U0[..., 4 + s]).sum()
+        m1 = interior(cfg, U[..., 4 + s]).sum()
+        assert abs(m1 - m0) <= 1e-9 * abs(m0), (s, m0, m1)
