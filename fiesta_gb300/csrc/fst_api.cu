@@ -442,6 +442,16 @@ int fst_create(const fst_config* cfg, fst_ctx** out) {
       e = cudaMemsetAsync(c->allocs[q], 0, c->alloc_bytes[q], c->stream);
     if (e != cudaSuccess) rc = cuda_fail(c, e, "cudaMemset");
   }
+  // FST_DEBUG_CANARY=1: the mixed path's primitive arrays start as NaN, so a
+  // read of an entry no kernel writes (row padding, halo beyond the grid)
+  // that reached an output would show up (tests compare against a normal run)
+  if (!rc && cfg->mode != FST_MODE_PLAIN_FP64) {
+    const char* cv = std::getenv("FST_DEBUG_CANARY");
+    if (cv && *cv == '1') {
+      e = fst_mixed_canary(g, c->bm, c->stream);
+      if (e != cudaSuccess) rc = cuda_fail(c, e, "canary fill");
+    }
+  }
   if (!rc) {
     e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);

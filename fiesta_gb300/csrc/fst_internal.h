@@ -154,6 +154,8 @@ struct MixedView {
 };
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);
+// Fill the primitive arrays with NaN bytes (debug canary, FST_DEBUG_CANARY)
+cudaError_t fst_mixed_canary(const Geo& g, const MixedBufs& b, cudaStream_t st);
 int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_alloc_fn& alloc,
                     std::string* why);
 int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs& b,

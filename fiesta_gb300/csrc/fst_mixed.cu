@@ -168,6 +168,22 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   return rc;
 }
 
+cudaError_t fst_mixed_canary(const Geo& g, const MixedBufs& b, cudaStream_t st) {
+  const size_t n = (size_t)b.gq.sv;
+  const struct {
+    void* p;
+    size_t bytes;
+  } f[] = {{b.Q, sizeof(float) * n * g.nv}, {b.rho32, sizeof(float) * n},
+           {b.vel32, sizeof(float) * n * g.ndim}, {b.mu32, sizeof(float) * n},
+           {b.T32, sizeof(float) * n}, {b.nrg, sizeof(float) * n},
+           {b.C, sizeof(float) * n * 5}, {b.p32, sizeof(float) * n * 2},
+           {b.p64, sizeof(double) * n}, {b.metf, sizeof(float) * n * 18}};
+  cudaError_t e = cudaSuccess;
+  for (const auto& x : f)
+    if (x.p && e == cudaSuccess) e = cudaMemsetAsync(x.p, 0xFF, x.bytes, st);
+  return e;
+}
+
 int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs& b,
                     const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
                     bool ghosts, cudaStream_t st, Prof* prof) {

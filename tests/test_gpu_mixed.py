@@ -147,3 +147,44 @@ def test_mixed_3d_term_combinations_ragged_tiles(ns, visc, ceq, buoy):
     for v, st, inc in field_errors(cfg, U, Ur, U0):
         assert st <= STATE_TOL, (v, st)
         assert inc <= INCR_TOL, (v, inc)
+
+
+@pytest.mark.parametrize("case", ["3d", "2d", "gen3d", "hybrid3d"])
+def test_gpu_nan_canary_never_reaches_outputs(case, monkeypatch):
+    """FST_DEBUG_CANARY=1 starts the primitive arrays as NaN: entries no
+    kernel writes (row padding of the TMA layout, halo beyond the grid) must
+    not reach the state, so two steps equal a normal run bit for bit."""
+    from tests.golden_io import wavy_nodes
+    sp = [dict(gamma=1.4, M=0.02896, mu=1.8e-5), dict(gamma=1.67, M=0.004, mu=1.99e-5)]
+    X = None
+    if case == "2d":
+        cfg = abi.make_config(2, (37, 29), dt=1e-4, species=[dict(gamma=1.4, M=1.0, mu=1e-3)],
+                              R=1.0, visc=True, ceq=True, mode=abi.MODE_MIXED)
+        U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 3)
+    elif case == "gen3d":
+        cfg = abi.make_config(3, (21, 18, 13), dx=(1.0, 1.0, 1.0), dt=1e-6, species=sp,
+                              grid_type=abi.GRID_GENERALIZED, mode=abi.MODE_MIXED)
+        U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 3, p_ambient=1e5, T_ambient=300.0,
+                                nkernels=3)
+        X = wavy_nodes(cfg, amp=0.2)
+    else:
+        mode = abi.MODE_HYBRID if case == "hybrid3d" else abi.MODE_MIXED
+        cfg = abi.make_config(3, (33, 20, 18), dt=5e-7, species=sp, visc=True, ceq=True,
+                              mode=mode)
+        U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 3, p_ambient=1e5, T_ambient=300.0,
+                                nkernels=3)
+
+    def run(canary):
+        monkeypatch.setenv("FST_DEBUG_CANARY", "1" if canary else "0")
+        s = Solver(cfg)
+        s.set_state(U0)
+        if X is not None:
+            s.apply_bcs()
+            s.set_grid(X)
+        s.rk_step(2)
+        U = s.get_state()
+        s.close()
+        return U
+
+    Un, Uc = run(False), run(True)
+    assert np.isfinite(Uc).all() and np.array_equal(Un, Uc)
