@@ -14,6 +14,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>  // header-only; ranges are no-ops without a tool attached
+
 #include "fst_common.cuh"
 #include "fst_internal.h"
 
@@ -293,6 +295,7 @@ int allocd(fst_ctx* c, T** p, size_t n) {
 
 int stage(fst_ctx* c, const double* Uin, const double* Uold, double* Unew, double coef,
           double* Rout, bool ghosts) {
+  nvtxRangePushA(Rout ? "fst rhs" : "fst rk stage");
   int n;
   if (c->cf.mode != FST_MODE_PLAIN_FP64)
     n = fst_mixed_stage(c->g, c->P, c->cf, c->bm, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
@@ -304,6 +307,7 @@ int stage(fst_ctx* c, const double* Uin, const double* Uold, double* Unew, doubl
     n = fst_plain2d_stage(c->g, c->P, c->b2, Uin, Uold, Unew, coef, Rout, ghosts, c->stream,
                           &c->prof);
   c->stats.kernel_launches += n;
+  nvtxRangePop();
   return check_launch(c, "stage kernels");
 }
 
