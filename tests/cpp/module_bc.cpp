@@ -1,7 +1,8 @@
 // Boundary-condition known answers through the C++ module interface
-// (include/fst_module.hpp): the values the reference's tests/bc_outflow.cpp
-// and tests/bc_reflective.cpp assert, on the same 3x3x3 grid with three
-// ghost layers.  Exit status 0 when every check holds.
+// (include/fst_module.hpp): the values the reference's tests/bc_outflow.cpp,
+// tests/bc_reflective.cpp, tests/bc_hydrostatic.cpp and the periodic case of
+// tests/test.cpp assert, on the same grids with three ghost layers.  Exit
+// status 0 when every check holds.
 #include <cstdio>
 
 #include "fst_module.hpp"
@@ -15,11 +16,12 @@ static int failures = 0;
     }                                                                \
   } while (0)
 
-static fst_config kat_config(int bc) {
+static fst_config kat_config(int bc, int nck = 3) {
   fst_config c;
   fst_config_defaults(&c);
   c.ndim = 3;
-  c.nci = c.ncj = c.nck = 3;
+  c.nci = c.ncj = 3;
+  c.nck = nck;
   c.dx = c.dy = c.dz = 1.0;
   c.dt = 1.0;
   c.R = 1.0;
@@ -65,6 +67,35 @@ int main() {
       CHECK(f.var(0, 4, 3, 0) == -6 && f.var(0, 4, 3, 1) == 6);
       CHECK(f.var(4, 8, 3, 0) == 2 && f.var(4, 8, 3, 1) == -2);
       CHECK(f.var(8, 4, 3, 0) == -4 && f.var(8, 4, 3, 1) == 4);
+    }
+    {  // hydrostatic in y: energy extrapolated from the first two interior rows
+      fst_config c = kat_config(FST_BC_OUTFLOW);
+      c.bc_ymin = c.bc_ymax = FST_BC_HYDROSTATIC;
+      fst::cart3d_func f(c);
+      int val = 1;
+      for (int j = 3; j <= 5; ++j)
+        for (int i = 3; i <= 5; ++i) {
+          f.var(i, j, 4, 3) = val++;
+          f.var(i, j, 4, 4) = 1.0;
+        }
+      f.upload();
+      fst::applyBCs(f);
+      f.download();
+      CHECK(f.var(4, 2, 4, 3) == -1 && f.var(4, 0, 4, 3) == -7 && f.var(0, 4, 4, 3) == 6);
+      CHECK(f.var(4, 8, 4, 3) == 17 && f.var(8, 4, 4, 3) == 4);
+      CHECK(f.var(0, 0, 4, 3) == -6 && f.var(8, 0, 4, 3) == -8);
+      CHECK(f.var(0, 8, 4, 3) == 18 && f.var(8, 8, 4, 3) == 16);
+    }
+    {  // periodic in x, y, z on a 3x3x10 interior
+      fst_config c = kat_config(FST_BC_REFLECTIVE, 10);
+      c.xper = c.yper = c.zper = 1;
+      fst::cart3d_func f(c);
+      for (int k = 3; k < 13; ++k) f.var(4, 4, k, 0) = 47 + k;  // 50 .. 59
+      f.upload();
+      fst::applyBCs(f);
+      f.download();
+      CHECK(f.var(4, 4, 0, 0) == 57 && f.var(4, 4, 1, 0) == 58 && f.var(4, 4, 2, 0) == 59);
+      CHECK(f.var(4, 4, 13, 0) == 50 && f.var(4, 4, 14, 0) == 51 && f.var(4, 4, 15, 0) == 52);
     }
     {  // the module choice and a rejected config
       fst_config c = kat_config(FST_BC_OUTFLOW);
