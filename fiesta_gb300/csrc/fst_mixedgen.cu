@@ -67,9 +67,7 @@ __global__ void __launch_bounds__(256) k_gen_tvel(Geo g, Geo gq, const float* __
 struct Pair {
   float h, l;
 };
-__device__ __forceinline__ Pair pm(const float* __restrict__ pp, const float* __restrict__ mf,
-                                   long long q, long long pv, long long mv) {
-  const float ph = pp[q], pl = pp[q + pv], mh = mf[q], ml = mf[q + mv];
+__device__ __forceinline__ Pair pm(float ph, float pl, float mh, float ml) {
   const float h = __fmul_rn(ph, mh);
   const float e = __fmaf_rn(ph, mh, -h);
   return {h, __fmaf_rn(pl, mh, __fmaf_rn(ph, ml, e))};
@@ -88,27 +86,36 @@ __global__ void __launch_bounds__(256) k_gen_cell(Geo g, Geo gq, MixedView M,
   const long long q = (long long)i + gq.sy * j + gq.sz * k;
   const long long c = (long long)i + g.sy * j + g.sz * k;
   const long long st[3] = {1, gq.sy, gq.sz};
-  const long long pv = gq.sv, mv = 9 * gq.sv;
-  float R[3];
+  const long long sv = gq.sv;
+  const float* ph = M.pp;
+  const float* pl = M.pp + sv;
+  float s[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-  for (int w = 0; w < 3; ++w) {
-    float s = 0.f;
+  for (int a = 0; a < 3; ++a) {
+    const long long o = st[a];
+    const long long pts[4] = {q - 2 * o, q - o, q + o, q + 2 * o};
+    Pair t[4][3];  // p*m(a, w) at the four points, each pressure read once
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float* mf = metf + gq.sv * (a + 3 * w);
-      const long long o = st[a];
-      const Pair m2 = pm(M.pp, mf, q - 2 * o, pv, mv), m1 = pm(M.pp, mf, q - o, pv, mv);
-      const Pair p1 = pm(M.pp, mf, q + o, pv, mv), p2 = pm(M.pp, mf, q + 2 * o, pv, mv);
-      // (t(-2) - 8 t(-1) + 8 t(+1) - t(+2)) / 12 with close values differenced first
-      const float A = __fadd_rn(__fsub_rn(p1.h, m1.h), __fsub_rn(p1.l, m1.l));
-      const float B = __fadd_rn(__fsub_rn(p2.h, m2.h), __fsub_rn(p2.l, m2.l));
-      s = __fadd_rn(s, __fmul_rn(__fmaf_rn(8.0f, A, -B), 1.0f / 12.0f));
+    for (int n = 0; n < 4; ++n) {
+      const long long x = pts[n];
+      const float h = ph[x], l = pl[x];
+#pragma unroll
+      for (int w = 0; w < 3; ++w) {
+        const float* mf = metf + sv * (a + 3 * w);
+        t[n][w] = pm(h, l, mf[x], mf[x + 9 * sv]);
+      }
     }
-    R[w] = -s;
+    // (t(-2) - 8 t(-1) + 8 t(+1) - t(+2)) / 12 with close values differenced first
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {
+      const float A = __fadd_rn(__fsub_rn(t[2][w].h, t[1][w].h), __fsub_rn(t[2][w].l, t[1][w].l));
+      const float B = __fadd_rn(__fsub_rn(t[3][w].h, t[0][w].h), __fsub_rn(t[3][w].l, t[0][w].l));
+      s[w] = __fadd_rn(s[w], __fmul_rn(__fmaf_rn(8.0f, A, -B), 1.0f / 12.0f));
+    }
   }
 #pragma unroll
   for (int w = 0; w < 3; ++w) {
-    const double r = (double)R[w];
+    const double r = (double)(-s[w]);
     const long long a = c + g.sv * w;
     if (Rout) Rout[a] = r;
     else Unew[a] = Uold[a] + coef * r;
