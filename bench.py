@@ -452,6 +452,67 @@ def cpu_sample_gen3d(n_sample=256, steps=1):
             "kind": "port", "sample": f"{steps} step(s) at {n_sample}^3 ({el:.1f} s)"}
 
 
+def run_aux(n, U0, dt, peak_gbs, peak_kind, reps=3, cpu=True):
+    """The postStep work beside the step, on the headline mixed context:
+    secondary variables (rho, p, T, velocity over all cells), the status
+    min/max reduction, and the noise filter (momenta, one sweep); device time
+    per call from the kernels' CUDA events, against the HBM roof, and the CPU
+    oracle on the same calls."""
+    import torch
+    from fiesta_gb300.solver import Solver
+    cfg = make_cfg(n, MODES["mixed"], dt)
+    s = Solver(cfg)
+    s.set_stream(torch.cuda.current_stream().cuda_stream)
+    s.set_state(U0)
+    s.secondary()
+    s.set_profiling(True)
+    s.kernel_times()
+    for _ in range(reps):
+        s.secondary()
+        s.status(secondary=False)
+        s.noise_filter(1e-3, 0.1, 0.5, 1, 1)
+    kt = s.kernel_times()
+    s.close()
+    allc = (n + 6) ** 3
+    inner = n ** 3
+    nv, nvt = 4 + cfg.ns, 4 + cfg.ns + 5
+    noise_ms = sum(v[1] for k, v in kt.items() if k.startswith("noise")) / reps
+    rows = {
+        # reads the state's nv fields, writes rho, p, u, v, w, T (FP64)
+        "secondary": (kt.get("secondary", (0, 0.0))[1] / reps, allc * 8 * (nv + 6)),
+        # reads the nvt state fields over the interior
+        "status": (kt.get("status", (0, 0.0))[1] / reps, inner * 8 * nvt),
+        # per filtered momentum: |C_hat| maximum, detection (variable + C_hat
+        # read, indicator written), one removal sweep (variable and indicator
+        # read, variable written)
+        "noise_filter": (noise_ms, 3 * inner * (8 + 8 + 8 + 4 + 8 + 4 + 8)),
+    }
+    out = {}
+    for k, (ms, b) in rows.items():
+        ach = b / (ms / 1e3) / 1e9 if ms > 0 else None
+        out[k] = {"ms_per_call": ms, "algorithmic_bytes": b, "achieved_gbs": ach,
+                  "hbm_frac": ach / peak_gbs if ach else None, "peak_source": peak_kind}
+    out["noise_filter"]["launches_per_call"] = sum(v[0] for k, v in kt.items()
+                                                   if k.startswith("noise")) // reps
+    if cpu:  # the oracle on the same calls (OpenMP; the noise filter's sweep is serial)
+        from oracle.oracle import Oracle
+        cores = os.cpu_count() or 1
+        Oracle.set_threads(cores)
+        o = Oracle(make_cfg(n, 0, dt))
+        o.set_state(U0)
+        t0 = time.perf_counter()
+        o.secondary()
+        t1 = time.perf_counter()
+        o.noise_filter(1e-3, 0.1, 0.5, 1, 1)
+        t2 = time.perf_counter()
+        out["cpu_oracle"] = {"cores": cores, "secondary_ms": (t1 - t0) * 1e3,
+                             "noise_filter_ms": (t2 - t1) * 1e3,
+                             "note": "secondary includes its host repack; the noise "
+                                     "filter's removal sweep is serial by definition"}
+    out["workload"] = f"{n}^3 mixing case, mixed context; noise filter mode 1 (momenta), nt = 1"
+    return out
+
+
 def accuracy_report(cfg, U0, finals, nsteps):
     """rel-L2 per conserved field over the interior, after the same steps:
     mixed and hybrid against the plain FP64 path (bit-identical to the
@@ -532,6 +593,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-gen", action="store_true")
+    ap.add_argument("--no-aux", action="store_true")
     a = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -617,6 +679,7 @@ def main():
         del Up, Um
         if not a.no_cpu:
             gen3d["cpu_baseline"] = cpu_sample_gen3d(min(n, a.cpu_sample))
+    aux = None if a.no_aux else run_aux(n, U0, dt, peak, peak_kind, cpu=not a.no_cpu)
     cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
@@ -641,6 +704,7 @@ def main():
         "modes": {m: {k: v for k, v in results[m].items() if k not in ("clocks",)} for m in modes},
         "batch2d": batch,
         "gen3d": gen3d,
+        "aux": aux,
         "accuracy": accuracy,
     }
     print(json.dumps(line))

@@ -642,6 +642,7 @@ int fst_secondary(fst_ctx* c, double* out, size_t n) {
   const int nf = g.ndim == 3 ? 6 : 5;
   if (n != nc * nf) return fail(c, FST_ERR_SIZE, "secondary size mismatch");
   const double *rho, *pr, *vel, *T;
+  c->prof.begin("secondary", c->stream);
   if (c->cf.mode != FST_MODE_PLAIN_FP64) {
     c->stats.kernel_launches += fst_mixed_secondary(g, c->P, c->bm, c->Ua, c->stream, &rho, &pr, &vel, &T);
   } else if (g.ndim == 3) {
@@ -651,6 +652,7 @@ int fst_secondary(fst_ctx* c, double* out, size_t n) {
     c->stats.kernel_launches += fst_plain2d_secondary(g, c->P, c->b2, c->Ua, c->stream);
     rho = c->b2.rho; pr = c->b2.pr; vel = c->b2.vel; T = c->b2.T;
   }
+  c->prof.end(c->stream);
   int rc = check_launch(c, "secondary");
   if (rc) return rc;
   const size_t B = nc * sizeof(double);
@@ -699,7 +701,9 @@ int fst_status(fst_ctx* c, double* vmin, double* vmax, double* xmin, double* xma
   cudaError_t e = cudaMemcpyAsync(c->dstat, init, sizeof(unsigned long long) * 2 * nf,
                                   cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "status init");
+  c->prof.begin("status", c->stream);
   k_status<<<dim3(152, nf), 256, 0, c->stream>>>(g, F, c->dstat);
+  c->prof.end(c->stream);
   c->stats.kernel_launches += 1;
   int rc = check_launch(c, "status");
   if (rc) return rc;
