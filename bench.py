@@ -667,16 +667,16 @@ def main():
         Um, gen3d["mixed"] = run_gen3d(n, a.steps, a.warmup, peak, peak_kind, 1)
         gcfg = gen3d_cfg(n, 1.0)
         ng, nsteps = gcfg.ng, a.warmup + a.steps
-        U0, _, _ = gen3d_state(gcfg, 1.0)
+        G0, _, _ = gen3d_state(gcfg, 1.0)
         rows = {}
         for v in range(Up.shape[3]):  # momenta by their increments (they start at zero)
-            z = U0[ng:-ng, ng:-ng, ng:-ng, v] if v < 3 else 0.0
+            z = G0[ng:-ng, ng:-ng, ng:-ng, v] if v < 3 else 0.0
             pa, ma = Up[ng:-ng, ng:-ng, ng:-ng, v] - z, Um[ng:-ng, ng:-ng, ng:-ng, v] - z
             nb = np.linalg.norm(pa.ravel())
             rows[v] = float(np.linalg.norm((ma - pa).ravel()) / nb) if nb > 0 else 0.0
         gen3d["mixed"]["rel_l2_vs_plain_after_steps"] = {"steps": nsteps, "max": max(rows.values()),
                                                           "per_variable": rows}
-        del Up, Um
+        del Up, Um, G0
         if not a.no_cpu:
             gen3d["cpu_baseline"] = cpu_sample_gen3d(min(n, a.cpu_sample))
     aux = None if a.no_aux else run_aux(n, U0, dt, peak, peak_kind, cpu=not a.no_cpu)
