@@ -113,3 +113,62 @@ def test_gpu_gen2d_noise_matches_oracle(case):
         o.noise_filter(dh, 0.1, 0.5, nt, mode)
         s.noise_filter(dh, 0.1, 0.5, nt, mode)
         assert same(s.get_state(), o.get_state())
+
+
+SPARSE_CASES = [  # ndim, cells, dh, nt: rough only in one box, a block of -0 momenta
+    (3, (40, 36, 33), 1e-2, 1),
+    (3, (40, 36, 33), 1e-2, 2),
+    (2, (70, 50), 3e-2, 1),
+]
+
+
+def _sparse_case(ndim, n, seed):
+    """A smooth state with one rough box (flagged cells in a few tiles only)
+    and a block of -0 momenta, where an unflagged update still turns -0 into
+    +0: the tiles the removal may skip sit beside ones it may not."""
+    sp = [dict(gamma=1.4, M=1.0, mu=1e-3)]
+    cfg = abi.make_config(ndim, n, dt=1e-4, species=sp, R=1.0, ceq=False)
+    rng = np.random.default_rng(seed)
+    U = np.array(initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, seed), order="F")
+    ng = 3
+    box = tuple(slice(ng + 9, ng + 15) for _ in range(ndim))
+    U[box] *= 1 + 0.05 * rng.standard_normal(U[box].shape)
+    U[tuple(slice(ng + 16, ng + 32) for _ in range(ndim)) + (slice(0, ndim),)] = -0.0
+    return cfg, U
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+@pytest.mark.skipif(not Reference.available(), reason="reference checker not built")
+@pytest.mark.parametrize("case", SPARSE_CASES)
+def test_oracle_sparse_noise_matches_reference(case):
+    ndim, n, dh, nt = case
+    cfg, U = _sparse_case(ndim, n, 8)
+    o, r = Oracle(cfg), Reference(cfg)
+    o.set_state(U)
+    r.set_state(U)
+    o.noise_filter(dh, 0.1, 0.0, nt, 1)
+    r.noise_filter(dh, 0.1, 0.0, nt, 1)
+    assert np.array_equal(_bits(o.get_state()), _bits(r.get_state()))
+    flagged = int(o.noise().sum())
+    assert 0 < flagged < o.noise().size // 4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", SPARSE_CASES)
+def test_gpu_sparse_noise_matches_oracle(case):
+    """Bit patterns, signed zeros included."""
+    from fiesta_gb300.solver import Solver
+    ndim, n, dh, nt = case
+    cfg, U = _sparse_case(ndim, n, 9)
+    o, s = Oracle(cfg), Solver(cfg)
+    o.set_state(U)
+    s.set_state(U)
+    for _ in range(2):
+        o.noise_filter(dh, 0.1, 0.0, nt, 1)
+        s.noise_filter(dh, 0.1, 0.0, nt, 1)
+        assert np.array_equal(_bits(s.get_state()), _bits(o.get_state()))
+    neg0 = _bits(U) == np.uint64(0x8000000000000000)
+    assert (neg0 & (_bits(o.get_state()) == 0)).any()  # some -0 became +0
