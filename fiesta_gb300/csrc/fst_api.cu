@@ -733,10 +733,11 @@ int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
   if (np->nt < 0) return fail(c, FST_ERR_INVALID, "noise nt must be >= 0");
   const Geo& g = c->g;
   if (!c->dnoise) {  // zero-initialised like the module's FS3D_I / FS2D_I
-    int rc = allocd(c, &c->dnoise, (size_t)g.sv);
+    const size_t ints = (size_t)fst_noise_ints(g);
+    int rc = allocd(c, &c->dnoise, ints);
     if (!rc) rc = allocd(c, &c->dnoise_key, 1);
     if (rc) return rc;
-    cudaError_t e = cudaMemsetAsync(c->dnoise, 0, sizeof(int) * (size_t)g.sv, c->stream);
+    cudaError_t e = cudaMemsetAsync(c->dnoise, 0, sizeof(int) * ints, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "noise init");
   }
   c->stats.kernel_launches +=

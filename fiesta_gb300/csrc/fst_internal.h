@@ -177,7 +177,9 @@ int fst_hybrid_pack(MixedBufs& b, const float* h_params, cudaStream_t st);
 int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
                     const double* U, cudaStream_t st);
 
-// fst_noise.cu: the postStep noise filter on state U
+// fst_noise.cu: the postStep noise filter on state U; `noise` holds
+// fst_noise_ints(g) ints (the indicator, then the removal's tile marks)
+long long fst_noise_ints(const Geo& g);
 int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
                      unsigned long long* key, const fst_noise_params& np, cudaStream_t st,
                      Prof* prof);

@@ -30,21 +30,22 @@
 namespace {
 
 constexpr int T3 = 8;   // 3D tile edge (cells)
-constexpr int T2 = 16;  // 2D tile edge
+constexpr int T2 = 32;  // 2D tile edge
 
 // max |var(cv)| over the interior into key (Kokkos Max semantics: strict
 // comparison from -DBL_MAX, NaN skipped)
 __global__ void __launch_bounds__(256) k_noise_maxabs(Geo g, const double* __restrict__ U, int cv,
                                                       unsigned long long* __restrict__ key) {
   const double* a = U + g.sv * cv;
-  const long long ni = g.nci, nj = g.ncj;
-  const long long n = ni * nj * (g.ndim == 3 ? g.nck : 1);
+  const int rows = g.ncj * (g.ndim == 3 ? g.nck : 1);
   double mx = -1.7976931348623157e308;
-  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
-       t += (long long)gridDim.x * 256) {
-    const long long i = t % ni, j = (t / ni) % nj, k = t / (ni * nj);
-    const double s = fabs(a[(i + g.ng) + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]);
-    if (s > mx) mx = s;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {  // one interior row per step
+    const int j = r % g.ncj, k = r / g.ncj;
+    const double* row = a + g.ng + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0);
+    for (int i = threadIdx.x; i < g.nci; i += 256) {
+      const double s = fabs(row[i]);
+      if (s > mx) mx = s;
+    }
   }
   mx = fst_warp_max(mx);
   __shared__ double sm[8];
@@ -67,6 +68,18 @@ __device__ __forceinline__ int last_centre(int o, int Mx) {
 // the filtered variables and the detection constants, computed on the host
 // with the reference's expressions (products and quotients only, so IEEE
 // rounding makes them the same there as on the device)
+// the weight of term n (planes k+1, k, k-1; rows j+1, j, j-1; columns i-1,
+// i, i+1) of the 3D detection stencil: -88 at the centre, 8 on the six face
+// neighbours, 2 elsewhere
+__device__ __forceinline__ double stencil_weight(int n) {
+  const int pk = n / 9, rj = (n / 3) % 3, ci = n % 3;
+  return pk == 1 ? (rj == 1 ? (ci == 1 ? -88.0 : 8.0) : (ci == 1 ? 8.0 : 2.0))
+                 : ((rj == 1 && ci == 1) ? 8.0 : 2.0);
+}
+
+// vars[q] without a local-memory copy of the kernel parameter
+__device__ __forceinline__ int pick(const int (&v)[3], int q) { return q == 0 ? v[0] : q == 1 ? v[1] : v[2]; }
+
 struct NoiseArgs {
   int nvars, vars[3], M, N, L, nvp1;
   double scale;   // 3D: sqrt(165 dx dy dz)/15840; 2D: sqrt(6 dx dy)/192
@@ -92,23 +105,31 @@ __global__ void __launch_bounds__(256) k_noise_detect(Geo g, const double* __res
   const int i = g.ng + 2 * ii, j = g.ng + 2 * jj, k = NDIM == 3 ? g.ng + 2 * kk : 0;
   unsigned hit = 0;
   for (int q = 0; q < A.nvars; ++q) {
-    const double* var = U + g.sv * A.vars[q];
+    const double* var = U + g.sv * pick(A.vars, q);
     double c;
     if (NDIM == 3) {
       // the reference's 27 terms in its order: planes k+1, k, k-1; rows j+1,
       // j, j-1; columns i-1, i, i+1
-      double sum = 0.0;
+      double t[27];
+      unsigned emax = 0;  // largest biased exponent of the 27 values
 #pragma unroll
-      for (int pk = 0; pk < 3; ++pk)
+      for (int n = 0; n < 27; ++n) {
+        const int pk = n / 9, rj = (n / 3) % 3, ci = n % 3;
+        t[n] = var[(long long)(i - 1 + ci) + g.sy * (j + 1 - rj) + g.sz * (k + 1 - pk)];
+        emax = max(emax, (unsigned)(__double_as_longlong(t[n]) >> 52) & 0x7ffu);
+      }
+      double sum = 2.0 * t[0];
+      if (emax < 1023 + 1020) {
+        // every |value| < 2^1020: the weights 2 and 8 scale exactly, so
+        // fma(w, v, sum) rounds sum + w*v once, as the reference's
+        // sum + (w*v) does -- the same bits for half the FP64 operations
 #pragma unroll
-        for (int rj = 0; rj < 3; ++rj)
+        for (int n = 1; n < 27; ++n)
+          sum = n == 13 ? sum + -88.0 * t[n] : __fma_rn(stencil_weight(n), t[n], sum);
+      } else {
 #pragma unroll
-          for (int ci = 0; ci < 3; ++ci) {
-            const double w = pk == 1 ? (rj == 1 ? (ci == 1 ? -88.0 : 8.0) : (ci == 1 ? 8.0 : 2.0))
-                                     : ((rj == 1 && ci == 1) ? 8.0 : 2.0);
-            const double tt = w * var[(long long)(i - 1 + ci) + g.sy * (j + 1 - rj) + g.sz * (k + 1 - pk)];
-            sum = (pk == 0 && rj == 0 && ci == 0) ? tt : sum + tt;
-          }
+        for (int n = 1; n < 27; ++n) sum = sum + stencil_weight(n) * t[n];
+      }
       c = -A.scale * sum;
     } else {
       auto V = [&](int x, int y) { return var[(long long)x + g.sy * y]; };
@@ -152,77 +173,238 @@ __device__ __forceinline__ bool unsafe_value(double x, long long safe) {
   return (b & 0x7fffffffffffffffll) >= safe || b == (long long)0x8000000000000000ull;
 }
 
-// One diagonal (tx+ty+tz = diag) of 8x8x8 interior tiles, 512 threads each,
-// every filtered variable in turn.
-__global__ void __launch_bounds__(T3* T3* T3) k_noise_remove3(Geo g, double* __restrict__ U,
-                                                              const int* __restrict__ noise,
-                                                              RemoveArgs R, int diag, int ntx,
-                                                              int nty, int ntz) {
+// OR of `bits` over the block, written by thread 0 to *out
+__device__ __forceinline__ void block_or_store(unsigned bits, int* out) {
+  __shared__ unsigned acc;
+  if (threadIdx.x == 0) acc = 0;
+  __syncthreads();
+  const unsigned w = __reduce_or_sync(0xffffffffu, bits);
+  if ((threadIdx.x & 31) == 0 && w) atomicOr(&acc, w);
+  __syncthreads();
+  if (threadIdx.x == 0) *out = (int)acc;
+}
+
+// The tiles a removal sweep must visit, bit q for variable vars[q]: a cell
+// flagged for q, or a value of q in the tile or its one-cell halo that
+// unsafe_value does not clear.  Any other tile is left bit for bit by the
+// sweep, as long as its halo stays safe: a visited tile that leaves an
+// unsafe value marks its face neighbours (k_noise_remove*).  One block per
+// tile, every tile in one launch.
+__global__ void __launch_bounds__(256) k_noise_tiles3(Geo g, const double* __restrict__ U,
+                                                      const int* __restrict__ noise,
+                                                      int* __restrict__ tiles, RemoveArgs R,
+                                                      int ntx, int nty) {
+  constexpr int E = T3 + 2, NL = (E * E * E + 255) / 256;
+  const int tx = blockIdx.x % ntx, ty = (blockIdx.x / ntx) % nty, tz = blockIdx.x / (ntx * nty);
+  const int i0 = g.ng + T3 * tx - 1, j0 = g.ng + T3 * ty - 1, k0 = g.ng + T3 * tz - 1;
+  const int xe = min(T3, g.ngi - g.ng - (i0 + 1)), ye = min(T3, g.ngj - g.ng - (j0 + 1)),
+            ze = min(T3, g.ngk - g.ng - (k0 + 1));
+  const int tid = threadIdx.x;
+  unsigned bits = 0;
+  for (int p = tid; p < T3 * T3 * T3; p += 256) {
+    const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
+    if (x < xe && y < ye && z < ze)
+      bits |= (unsigned)noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y) + g.sz * (k0 + 1 + z)];
+  }
+  bits &= (1u << R.nvars) - 1;
+  for (int q = 0; q < R.nvars; ++q) {
+    const double* var = U + g.sv * pick(R.vars, q);
+    bool bad = false;
+#pragma unroll
+    for (int u = 0; u < NL; ++u) {
+      const int p = tid + 256 * u;
+      const int x = i0 + p % E, y = j0 + (p / E) % E, z = k0 + p / (E * E);
+      if (p < E * E * E && x < g.ngi && y < g.ngj && z < g.ngk)
+        bad = bad || unsafe_value(var[(long long)x + g.sy * y + g.sz * z], R.safe);
+    }
+    if (bad) bits |= 1u << q;
+  }
+  block_or_store(bits, tiles + blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) k_noise_tiles2(Geo g, const double* __restrict__ U,
+                                                      const int* __restrict__ noise,
+                                                      int* __restrict__ tiles, RemoveArgs R,
+                                                      int ntx) {
+  constexpr int E = T2 + 2, NL = (E * E + 255) / 256;
+  const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+  const int i0 = g.ng + T2 * tx - 1, j0 = g.ng + T2 * ty - 1;
+  const int xe = min(T2, g.ngi - g.ng - (i0 + 1)), ye = min(T2, g.ngj - g.ng - (j0 + 1));
+  const int tid = threadIdx.x;
+  unsigned bits = 0;
+  for (int p = tid; p < T2 * T2; p += 256) {
+    const int x = p % T2, y = p / T2;
+    if (x < xe && y < ye) bits |= (unsigned)noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y)];
+  }
+  bits &= (1u << R.nvars) - 1;
+  for (int q = 0; q < R.nvars; ++q) {
+    const double* var = U + g.sv * pick(R.vars, q);
+    bool bad = false;
+#pragma unroll
+    for (int u = 0; u < NL; ++u) {
+      const int p = tid + 256 * u;
+      const int x = i0 + p % E, y = j0 + p / E;
+      if (p < E * E && x < g.ngi && y < g.ngj)
+        bad = bad || unsafe_value(var[(long long)x + g.sy * y], R.safe);
+    }
+    if (bad) bits |= 1u << q;
+  }
+  block_or_store(bits, tiles + blockIdx.x);
+}
+
+// after a visited tile's update: if it left a value unsafe for its
+// neighbours' skip (non-finite or large; -0 matters to its own cells only),
+// mark the face neighbours for variable q -- later diagonals of this sweep
+// and, for the earlier ones, the next sweep
+__device__ __forceinline__ bool hard_value(double x, long long safe) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffll) >= safe;
+}
+
+// cells of an 8-cube with x+y+z = s, ordered by z then y: those in plane z
+// number c(s - z), c(u) = min(u, 7) - max(0, u - 7) + 1 for 0 <= u <= 14
+__device__ __forceinline__ int row_cells(int u) {
+  return u < 0 || u > 2 * T3 - 2 ? 0 : min(u, T3 - 1) - max(0, u - (T3 - 1)) + 1;
+}
+
+constexpr int R3 = 256;  // threads per 3D tile (a wavefront holds at most 48 cells)
+
+// One diagonal (tx+ty+tz = diag) of 8x8x8 interior tiles, every filtered
+// variable in turn.  Inside a busy tile, wavefront w's cells go to
+// consecutive threads (a table in shared memory, built when first needed),
+// so the FP64 work of a step occupies ceil(cells/32) warps rather than
+// every warp the wavefront crosses.
+__global__ void __launch_bounds__(R3, 4) k_noise_remove3(Geo g, double* __restrict__ U,
+                                                         const int* __restrict__ noise,
+                                                         int* __restrict__ tiles, RemoveArgs R,
+                                                         int diag, int ntx, int nty, int ntz) {
   const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx, tz = diag - tx - ty;
   if (tz < 0 || tz >= ntz) return;  // uniform over the block
-  constexpr int E = T3 + 2;
-  __shared__ double s[E][E][E];  // [z][y][x], tile + one-cell halo
-  const int lx = threadIdx.x, ly = threadIdx.y, lz = threadIdx.z;
+  const int tile = blockIdx.x + ntx * nty * tz;
+  const int cand = tiles[tile];
+  if (!cand) return;  // no variable to visit (k_noise_tiles3)
+  constexpr int E = T3 + 2, C = T3 * T3 * T3, W = 3 * T3 - 2, NL = (E * E * E + R3 - 1) / R3;
+  __shared__ double s[E][E][E];          // [z][y][x], tile + one-cell halo
+  __shared__ int msk[C];                 // indicator of the tile's cells (0 outside)
+  __shared__ unsigned short order[C];    // cells (x + 8y + 64z) by wavefront
+  __shared__ short off[W + 1];           // wavefront w: order[off[w] .. off[w+1])
+  const int tid = threadIdx.x;
   const int i0 = g.ng + T3 * tx - 1, j0 = g.ng + T3 * ty - 1, k0 = g.ng + T3 * tz - 1;
-  const int tid = lx + T3 * (ly + T3 * lz);
-  const int i = i0 + 1 + lx, j = j0 + 1 + ly, k = k0 + 1 + lz;
-  const bool in = i < g.ngi - g.ng && j < g.ngj - g.ng && k < g.ngk - g.ng;
-  const long long cell = (long long)i + g.sy * j + g.sz * k;
-  const int nzm = in ? noise[cell] : 0;
+  const int xe = min(T3, g.ngi - g.ng - (i0 + 1)), ye = min(T3, g.ngj - g.ng - (j0 + 1)),
+            ze = min(T3, g.ngk - g.ng - (k0 + 1));  // interior extent of the tile
+  for (int p = tid; p < C; p += R3) {
+    const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
+    msk[p] = x < xe && y < ye && z < ze
+                 ? noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y) + g.sz * (k0 + 1 + z)]
+                 : 0;
+  }
   const double D = R.dx * R.dx + R.dy * R.dy + R.dz * R.dz;
+  bool table = false;
   for (int q = 0; q < R.nvars; ++q) {
-    double* var = U + g.sv * R.vars[q];
-    bool busy = in && ((nzm >> q) & 1);
-    __syncthreads();  // the previous variable's tile is stored
-    for (int p = tid; p < E * E * E; p += T3 * T3 * T3) {
+    if (!((cand >> q) & 1)) continue;
+    double* var = U + g.sv * pick(R.vars, q);
+    __syncthreads();  // msk is written; the previous variable's tile is stored
+    bool busy = false;
+    for (int p = tid; p < C; p += R3) busy = busy || ((msk[p] >> q) & 1);
+    double v[NL];
+#pragma unroll
+    for (int u = 0; u < NL; ++u) {  // every load in flight before the first store
+      const int p = tid + u * R3;
       const int a = p % E, b = (p / E) % E, c = p / (E * E);
       const int x = i0 + a, y = j0 + b, z = k0 + c;
-      if (x < g.ngi && y < g.ngj && z < g.ngk) {
-        const double val = var[(long long)x + g.sy * y + g.sz * z];
-        s[c][b][a] = val;
-        busy = busy || unsafe_value(val, R.safe);
+      if (p < E * E * E && x < g.ngi && y < g.ngj && z < g.ngk)
+        v[u] = var[(long long)x + g.sy * y + g.sz * z];
+    }
+#pragma unroll
+    for (int u = 0; u < NL; ++u) {
+      const int p = tid + u * R3;
+      const int a = p % E, b = (p / E) % E, c = p / (E * E);
+      if (p < E * E * E && i0 + a < g.ngi && j0 + b < g.ngj && k0 + c < g.ngk) {
+        s[c][b][a] = v[u];
+        busy = busy || unsafe_value(v[u], R.safe);
       }
     }
     if (!__syncthreads_or(busy)) continue;
-    const double nz = (double)((nzm >> q) & 1);
-    for (int w = 0; w < 3 * T3 - 2; ++w) {
-      if (in && lx + ly + lz == w) {
-        const int a = lx + 1, b = ly + 1, c = lz + 1;
-        const double lap = (s[c][b][a - 1] - 2 * s[c][b][a] + s[c][b][a + 1]) / (R.dx * R.dx) +
-                           (s[c][b - 1][a] - 2 * s[c][b][a] + s[c][b + 1][a]) / (R.dy * R.dy) +
-                           (s[c - 1][b][a] - 2 * s[c][b][a] + s[c + 1][b][a]) / (R.dz * R.dz);
-        const double dnoise = R.eta * D * nz * lap;
-        s[c][b][a] += dnoise;
+    if (!table) {  // cells with x+y+z = w ordered by z then y
+      if (tid <= W) {
+        int o = 0;
+        for (int z = 0; z < T3; ++z)
+          for (int w = 0; w < tid; ++w) o += row_cells(w - z);
+        off[tid] = (short)o;
+      }
+      __syncthreads();
+      for (int p = tid; p < C; p += R3) {
+        const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3), w = x + y + z;
+        int r = off[w] + y - max(0, w - z - (T3 - 1));
+        for (int zz = 0; zz < z; ++zz) r += row_cells(w - zz);
+        order[r] = (unsigned short)p;
+      }
+      __syncthreads();
+      table = true;
+    }
+    for (int w = 0; w < W; ++w) {
+      const int t = off[w] + tid;
+      if (t < off[w + 1]) {
+        const int p = order[t];
+        const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
+        if (x < xe && y < ye && z < ze) {
+          const int a = x + 1, b = y + 1, c = z + 1;
+          const double nz = (double)((msk[p] >> q) & 1);
+          const double lap = (s[c][b][a - 1] - 2 * s[c][b][a] + s[c][b][a + 1]) / (R.dx * R.dx) +
+                             (s[c][b - 1][a] - 2 * s[c][b][a] + s[c][b + 1][a]) / (R.dy * R.dy) +
+                             (s[c - 1][b][a] - 2 * s[c][b][a] + s[c + 1][b][a]) / (R.dz * R.dz);
+          const double dnoise = R.eta * D * nz * lap;
+          s[c][b][a] += dnoise;
+        }
       }
       __syncthreads();
     }
-    if (in) var[cell] = s[lz + 1][ly + 1][lx + 1];
+    bool hard = false;
+    for (int p = tid; p < C; p += R3) {
+      const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
+      if (x < xe && y < ye && z < ze) {
+        const double val = s[z + 1][y + 1][x + 1];
+        var[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y) + g.sz * (k0 + 1 + z)] = val;
+        hard = hard || hard_value(val, R.safe);
+      }
+    }
+    if (__syncthreads_or(hard) && tid < 6) {  // mark the face neighbours
+      const int ax = tid >> 1, d = (tid & 1) ? 1 : -1;
+      const int nx = tx + (ax == 0 ? d : 0), ny = ty + (ax == 1 ? d : 0), nz = tz + (ax == 2 ? d : 0);
+      if (nx >= 0 && nx < ntx && ny >= 0 && ny < nty && nz >= 0 && nz < ntz)
+        atomicOr(tiles + nx + ntx * (ny + nty * nz), 1 << q);
+    }
   }
 }
 
-// One diagonal (tx+ty = diag) of 16x16 interior tiles, 256 threads each,
-// every filtered variable in turn.
-__global__ void __launch_bounds__(T2* T2) k_noise_remove2(Geo g, double* __restrict__ U,
-                                                          const int* __restrict__ noise,
-                                                          RemoveArgs R, int diag, int nty) {
+// One diagonal (tx+ty = diag) of 32x32 interior tiles, one warp each, every
+// filtered variable in turn: lane t takes the t-th cell of wavefront w.
+__global__ void __launch_bounds__(32) k_noise_remove2(Geo g, double* __restrict__ U,
+                                                      const int* __restrict__ noise,
+                                                      int* __restrict__ tiles, RemoveArgs R,
+                                                      int diag, int ntx, int nty) {
   const int tx = blockIdx.x, ty = diag - tx;
   if (ty < 0 || ty >= nty) return;
+  const int cand = tiles[tx + ntx * ty];
+  if (!cand) return;  // no variable to visit (k_noise_tiles2)
   constexpr int E = T2 + 2;
   __shared__ double s[E][E];  // [y][x]
-  const int lx = threadIdx.x, ly = threadIdx.y;
+  __shared__ int msk[T2 * T2];
+  const int tid = threadIdx.x;
   const int i0 = g.ng + T2 * tx - 1, j0 = g.ng + T2 * ty - 1;
-  const int tid = lx + T2 * ly;
-  const int i = i0 + 1 + lx, j = j0 + 1 + ly;
-  const bool in = i < g.ngi - g.ng && j < g.ngj - g.ng;
-  const long long cell = (long long)i + g.sy * j;
-  const int nzm = in ? noise[cell] : 0;
+  const int xe = min(T2, g.ngi - g.ng - (i0 + 1)), ye = min(T2, g.ngj - g.ng - (j0 + 1));
+  for (int p = tid; p < T2 * T2; p += 32) {
+    const int x = p % T2, y = p / T2;
+    msk[p] = x < xe && y < ye ? noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y)] : 0;
+  }
   const double dx = R.dx, dy = R.dy;
   const double D = dx * dx + dy * dy;
   for (int q = 0; q < R.nvars; ++q) {
-    double* var = U + g.sv * R.vars[q];
-    bool busy = in && ((nzm >> q) & 1);
+    if (!((cand >> q) & 1)) continue;
+    double* var = U + g.sv * pick(R.vars, q);
+    bool busy = false;
     __syncthreads();
-    for (int p = tid; p < E * E; p += T2 * T2) {
+    for (int p = tid; p < T2 * T2; p += 32) busy = busy || ((msk[p] >> q) & 1);
+    for (int p = tid; p < E * E; p += 32) {
       const int a = p % E, b = p / E;
       const int x = i0 + a, y = j0 + b;
       if (x < g.ngi && y < g.ngj) {
@@ -232,10 +414,11 @@ __global__ void __launch_bounds__(T2* T2) k_noise_remove2(Geo g, double* __restr
       }
     }
     if (!__syncthreads_or(busy)) continue;
-    const double nz = (double)((nzm >> q) & 1);
     for (int w = 0; w < 2 * T2 - 1; ++w) {
-      if (in && lx + ly == w) {
-        const int a = lx + 1, b = ly + 1;
+      const int y = max(0, w - (T2 - 1)) + tid, x = w - y;  // x >= 0 while y <= w
+      if (x >= 0 && y < ye && x < xe) {
+        const int a = x + 1, b = y + 1;
+        const double nz = (double)((msk[x + T2 * y] >> q) & 1);
         const double lgrad = (s[b][a] - s[b][a - 1]) / dx;
         const double rgrad = (s[b][a + 1] - s[b][a]) / dx;
         const double bgrad = (s[b][a] - s[b - 1][a]) / dy;
@@ -243,9 +426,22 @@ __global__ void __launch_bounds__(T2* T2) k_noise_remove2(Geo g, double* __restr
         const double dv = R.eta * D * nz * ((rgrad - lgrad) / dx + (tgrad - bgrad) / dy);
         s[b][a] += dv;
       }
-      __syncthreads();
+      __syncwarp();
     }
-    if (in) var[cell] = s[ly + 1][lx + 1];
+    bool hard = false;
+    for (int p = tid; p < T2 * T2; p += 32) {
+      const int x = p % T2, y = p / T2;
+      if (x < xe && y < ye) {
+        const double val = s[y + 1][x + 1];
+        var[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y)] = val;
+        hard = hard || hard_value(val, R.safe);
+      }
+    }
+    if (__syncthreads_or(hard) && tid < 4) {  // mark the face neighbours
+      const int d = (tid & 1) ? 1 : -1;
+      const int nx = tx + (tid < 2 ? d : 0), ny = ty + (tid < 2 ? 0 : d);
+      if (nx >= 0 && nx < ntx && ny >= 0 && ny < nty) atomicOr(tiles + nx + ntx * ny, 1 << q);
+    }
   }
 }
 
@@ -266,6 +462,13 @@ inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 }  // namespace
 
+long long fst_noise_ints(const Geo& g) {
+  const long long tiles = g.ndim == 3 ? (long long)((g.nci + T3 - 1) / T3) * ((g.ncj + T3 - 1) / T3) *
+                                            ((g.nck + T3 - 1) / T3)
+                                      : (long long)((g.nci + T2 - 1) / T2) * ((g.ncj + T2 - 1) / T2);
+  return g.sv + tiles;
+}
+
 int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
                      unsigned long long* key, const fst_noise_params& np, cudaStream_t st,
                      Prof* prof) {
@@ -285,7 +488,7 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
     cudaMemcpyAsync(key, &init, sizeof(init), cudaMemcpyHostToDevice, st);
     // 3D: maxCvar3D(var, 6), a fixed index (src/cart3d.cpp:346); 2D: C_hat
     const int cv = g.ndim == 3 ? 6 : g.nv + 1;
-    FST_LAUNCH(prof, "noise_max", st, n, k_noise_maxabs<<<152, 256, 0, st>>>(g, U, cv, key));
+    FST_LAUNCH(prof, "noise_max", st, n, k_noise_maxabs<<<4 * 152, 256, 0, st>>>(g, U, cv, key));
   }
   NoiseArgs A{};
   if (np.mode == 1 || g2)
@@ -317,18 +520,24 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
   }
   RemoveArgs R{A.nvars, {A.vars[0], A.vars[1], A.vars[2]}, np.eta, dx, dy, dz,
                skip_bound(np.eta, dx, dy, g.ndim == 3 ? dz : dy)};
-  for (int tau = 0; tau < np.nt; ++tau) {
+  int* tiles = noise + g.sv;  // candidate tiles (fst_noise_ints)
+  if (np.nt > 0) {
     if (g.ndim == 3) {
       const int ntx = (g.nci + T3 - 1) / T3, nty = (g.ncj + T3 - 1) / T3, ntz = (g.nck + T3 - 1) / T3;
-      for (int d = 0; d <= ntx + nty + ntz - 3; ++d)
-        FST_LAUNCH(prof, "noise_remove", st, n,
-                   k_noise_remove3<<<ntx * nty, dim3(T3, T3, T3), 0, st>>>(g, U, noise, R, d, ntx,
-                                                                           nty, ntz));
+      FST_LAUNCH(prof, "noise_tiles", st, n,
+                 k_noise_tiles3<<<ntx * nty * ntz, 256, 0, st>>>(g, U, noise, tiles, R, ntx, nty));
+      for (int tau = 0; tau < np.nt; ++tau)
+        for (int d = 0; d <= ntx + nty + ntz - 3; ++d)
+          FST_LAUNCH(prof, "noise_remove", st, n,
+                     k_noise_remove3<<<ntx * nty, R3, 0, st>>>(g, U, noise, tiles, R, d, ntx, nty, ntz));
     } else {
       const int ntx = (g.nci + T2 - 1) / T2, nty = (g.ncj + T2 - 1) / T2;
-      for (int d = 0; d <= ntx + nty - 2; ++d)
-        FST_LAUNCH(prof, "noise_remove", st, n,
-                   k_noise_remove2<<<ntx, dim3(T2, T2), 0, st>>>(g, U, noise, R, d, nty));
+      FST_LAUNCH(prof, "noise_tiles", st, n,
+                 k_noise_tiles2<<<ntx * nty, 256, 0, st>>>(g, U, noise, tiles, R, ntx));
+      for (int tau = 0; tau < np.nt; ++tau)
+        for (int d = 0; d <= ntx + nty - 2; ++d)
+          FST_LAUNCH(prof, "noise_remove", st, n,
+                     k_noise_remove2<<<ntx, 32, 0, st>>>(g, U, noise, tiles, R, d, ntx, nty));
     }
   }
   return n;

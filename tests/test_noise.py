@@ -115,17 +115,22 @@ def test_gpu_gen2d_noise_matches_oracle(case):
         assert same(s.get_state(), o.get_state())
 
 
-SPARSE_CASES = [  # ndim, cells, dh, nt: rough only in one box, a block of -0 momenta
-    (3, (40, 36, 33), 1e-2, 1),
-    (3, (40, 36, 33), 1e-2, 2),
-    (2, (70, 50), 3e-2, 1),
+SPARSE_CASES = [  # ndim, cells, dh, nt, planted: rough in one box, a block of -0 momenta
+    (3, (40, 36, 33), 1e-2, 1, None),
+    (3, (40, 36, 33), 1e-2, 2, None),
+    (2, (70, 50), 3e-2, 1, None),
+    (3, (40, 36, 33), 1e-2, 2, "nan"),
+    (3, (40, 36, 33), 1e-2, 1, "huge"),
+    (2, (70, 50), 3e-2, 2, "nan"),
 ]
 
 
-def _sparse_case(ndim, n, seed):
+def _sparse_case(ndim, n, seed, planted=None):
     """A smooth state with one rough box (flagged cells in a few tiles only)
     and a block of -0 momenta, where an unflagged update still turns -0 into
-    +0: the tiles the removal may skip sit beside ones it may not."""
+    +0: the tiles the removal may skip sit beside ones it may not.  `planted`
+    puts a NaN or a near-overflow value in an unflagged region, whose
+    non-finite results then spread through the sweep across tiles."""
     sp = [dict(gamma=1.4, M=1.0, mu=1e-3)]
     cfg = abi.make_config(ndim, n, dt=1e-4, species=sp, R=1.0, ceq=False)
     rng = np.random.default_rng(seed)
@@ -133,7 +138,11 @@ def _sparse_case(ndim, n, seed):
     ng = 3
     box = tuple(slice(ng + 9, ng + 15) for _ in range(ndim))
     U[box] *= 1 + 0.05 * rng.standard_normal(U[box].shape)
-    U[tuple(slice(ng + 16, ng + 32) for _ in range(ndim)) + (slice(0, ndim),)] = -0.0
+    k = () if ndim == 3 else (0,)  # the 2D state is (ngi, ngj, 1, nvt)
+    U[tuple(slice(ng + 16, ng + 32) for _ in range(ndim)) + k + (slice(0, ndim),)] = -0.0
+    if planted:
+        at = (ng + 34, ng + 2) + ((ng + 20,) if ndim == 3 else k)
+        U[at + (1,)] = np.nan if planted == "nan" else 1e305
     return cfg, U
 
 
@@ -141,34 +150,41 @@ def _bits(a):
     return np.ascontiguousarray(a).view(np.uint64)
 
 
+def _same_bits(a, b):
+    """Bit patterns, signed zeros included; NaN matches NaN whatever its payload."""
+    nan = np.isnan(a) & np.isnan(b)
+    return same(a, b) and np.array_equal(_bits(a)[~nan], _bits(b)[~nan])
+
+
 @pytest.mark.skipif(not Reference.available(), reason="reference checker not built")
 @pytest.mark.parametrize("case", SPARSE_CASES)
 def test_oracle_sparse_noise_matches_reference(case):
-    ndim, n, dh, nt = case
-    cfg, U = _sparse_case(ndim, n, 8)
+    ndim, n, dh, nt, planted = case
+    cfg, U = _sparse_case(ndim, n, 8, planted)
     o, r = Oracle(cfg), Reference(cfg)
     o.set_state(U)
     r.set_state(U)
     o.noise_filter(dh, 0.1, 0.0, nt, 1)
     r.noise_filter(dh, 0.1, 0.0, nt, 1)
-    assert np.array_equal(_bits(o.get_state()), _bits(r.get_state()))
+    assert _same_bits(o.get_state(), r.get_state())
     flagged = int(o.noise().sum())
     assert 0 < flagged < o.noise().size // 4
+    if planted:  # the sweep carried non-finite values past the planted cell
+        assert int((~np.isfinite(o.get_state())).sum()) > 1
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", SPARSE_CASES)
 def test_gpu_sparse_noise_matches_oracle(case):
-    """Bit patterns, signed zeros included."""
     from fiesta_gb300.solver import Solver
-    ndim, n, dh, nt = case
-    cfg, U = _sparse_case(ndim, n, 9)
+    ndim, n, dh, nt, planted = case
+    cfg, U = _sparse_case(ndim, n, 9, planted)
     o, s = Oracle(cfg), Solver(cfg)
     o.set_state(U)
     s.set_state(U)
     for _ in range(2):
         o.noise_filter(dh, 0.1, 0.0, nt, 1)
         s.noise_filter(dh, 0.1, 0.0, nt, 1)
-        assert np.array_equal(_bits(s.get_state()), _bits(o.get_state()))
+        assert _same_bits(s.get_state(), o.get_state())
     neg0 = _bits(U) == np.uint64(0x8000000000000000)
     assert (neg0 & (_bits(o.get_state()) == 0)).any()  # some -0 became +0
