@@ -482,10 +482,9 @@ def run_aux(n, U0, dt, peak_gbs, peak_kind, reps=3, cpu=True):
         "secondary": (kt.get("secondary", (0, 0.0))[1] / reps, allc * 8 * (nv + 6)),
         # reads the nvt state fields over the interior
         "status": (kt.get("status", (0, 0.0))[1] / reps, inner * 8 * nvt),
-        # per filtered momentum: |C_hat| maximum, detection (variable + C_hat
-        # read, indicator written), one removal sweep (variable and indicator
-        # read, variable written)
-        "noise_filter": (noise_ms, 3 * inner * (8 + 8 + 8 + 4 + 8 + 4 + 8)),
+        # compulsory: the cutoff's C variable (maximum), the three momenta once,
+        # the indicator written; a sweep that changes no cell moves nothing more
+        "noise_filter": (noise_ms, inner * (8 + 3 * 8 + 4)),
     }
     out = {}
     for k, (ms, b) in rows.items():
