@@ -249,16 +249,30 @@ struct StatusFields {
 __global__ void __launch_bounds__(256) k_status(Geo g, StatusFields F,
                                                 unsigned long long* __restrict__ keys) {
   const double* a = F.f[blockIdx.y];
-  const long long ni = g.nci, nj = g.ncj;
-  const long long n = ni * nj * (g.ndim == 3 ? g.nck : 1);
-  double mx = -1.7976931348623157e308, mn = 1.7976931348623157e308;
-  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
-       t += (long long)gridDim.x * 256) {
-    const long long i = t % ni, j = (t / ni) % nj, k = t / (ni * nj);
-    const double v = a[(i + g.ng) + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)];
-    if (v > mx) mx = v;
-    if (v < mn) mn = v;
-  }
+  const int rows = g.ncj * (g.ndim == 3 ? g.nck : 1);
+  // per-thread extremes on the order-preserving integer key: FP64 compares
+  // would run on the FP64 pipe, two per value; NaN is skipped, as by the
+  // reference's `if (v > max)` reducers
+  unsigned long long kmx = FST_KEY_LOWEST, kmn = 0xFFEFFFFFFFFFFFFFull;  // keys of -+DBL_MAX
+  constexpr int RB = 4;  // interior rows per step, their loads in flight together
+  for (int r0 = blockIdx.x * RB; r0 < rows; r0 += gridDim.x * RB)
+    for (int i = threadIdx.x; i < g.nci; i += 256) {
+      unsigned long long v[RB];
+#pragma unroll
+      for (int u = 0; u < RB; ++u) {
+        const int r = r0 + u < rows ? r0 + u : 0, j = r % g.ncj, k = r / g.ncj;  // past the end: row 0
+        v[u] = (unsigned long long)__double_as_longlong(
+            a[g.ng + i + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]);
+      }
+#pragma unroll
+      for (int u = 0; u < RB; ++u) {
+        if ((v[u] & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) continue;  // NaN
+        const unsigned long long key = (v[u] >> 63) ? ~v[u] : (v[u] | 0x8000000000000000ull);
+        kmx = key > kmx ? key : kmx;
+        kmn = key < kmn ? key : kmn;
+      }
+    }
+  double mx = fst_unkey(kmx), mn = fst_unkey(kmn);
   __shared__ double smx[8], smn[8];
   mx = fst_warp_max(mx);
   mn = -fst_warp_max(-mn);

@@ -28,38 +28,44 @@ namespace {
 
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 
+// Both per-cell kernels below run one block per grid row (j, k), ghosts
+// included, threads along i.
+
 // metric (a, b) of a cell as FP32 hi [9 fields] and lo [9 fields]
-__global__ void __launch_bounds__(256) k_metric_pair(Geo g, Geo gq, const double* __restrict__ met,
+__global__ void __launch_bounds__(128) k_metric_pair(Geo g, Geo gq, const double* __restrict__ met,
                                                      float* __restrict__ metf) {
-  const long long c = (long long)blockIdx.x * 256 + threadIdx.x;
-  if (c >= g.sv) return;
-  const int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj), k = (int)(c / g.sz);
-  const long long q = (long long)i + gq.sy * j + gq.sz * k;
+  const int j = (int)(blockIdx.x % g.ngj), k = (int)(blockIdx.x / g.ngj);
+  for (int i = threadIdx.x; i < g.ngi; i += 128) {
+    const long long c = (long long)i + g.sy * j + g.sz * k;
+    const long long q = (long long)i + gq.sy * j + gq.sz * k;
 #pragma unroll
-  for (int n = 0; n < 9; ++n) {
-    const double m = met[c + g.sv * n];
-    const float h = __double2float_rn(m);
-    metf[q + gq.sv * n] = h;
-    metf[q + gq.sv * (9 + n)] = __double2float_rn(m - (double)h);
+    for (int n = 0; n < 9; ++n) {
+      const double m = met[c + g.sv * n];
+      const float h = __double2float_rn(m);
+      metf[q + gq.sv * n] = h;
+      metf[q + gq.sv * (9 + n)] = __double2float_rn(m - (double)h);
+    }
   }
 }
 
 // contravariant velocity over every cell (ghosts included: the face
 // kernels' stencils read them), in place
-__global__ void __launch_bounds__(256) k_gen_tvel(Geo g, Geo gq, const float* __restrict__ metf,
+__global__ void __launch_bounds__(128) k_gen_tvel(Geo gq, int ngi, int ngj,
+                                                  const float* __restrict__ metf,
                                                   float* __restrict__ vel) {
-  const long long c = (long long)blockIdx.x * 256 + threadIdx.x;
-  if (c >= g.sv) return;
-  const int i = (int)(c % g.sy), j = (int)((c / g.sy) % g.ngj), k = (int)(c / g.sz);
-  const long long q = (long long)i + gq.sy * j + gq.sz * k, sv = gq.sv;
-  const float u0 = vel[q], u1 = vel[q + sv], u2 = vel[q + 2 * sv];
-  float t[3];
+  const int j = (int)(blockIdx.x % ngj), k = (int)(blockIdx.x / ngj);
+  const long long sv = gq.sv;
+  for (int i = threadIdx.x; i < ngi; i += 128) {
+    const long long q = (long long)i + gq.sy * j + gq.sz * k;
+    const float u0 = vel[q], u1 = vel[q + sv], u2 = vel[q + 2 * sv];
+    float t[3];
 #pragma unroll
-  for (int a = 0; a < 3; ++a)  // m(a, b) at field a + 3b
-    t[a] = __fmaf_rn(metf[q + sv * (a + 6)], u2,
-                     __fmaf_rn(metf[q + sv * (a + 3)], u1, __fmul_rn(metf[q + sv * a], u0)));
+    for (int a = 0; a < 3; ++a)  // m(a, b) at field a + 3b
+      t[a] = __fmaf_rn(metf[q + sv * (a + 6)], u2,
+                       __fmaf_rn(metf[q + sv * (a + 3)], u1, __fmul_rn(metf[q + sv * a], u0)));
 #pragma unroll
-  for (int a = 0; a < 3; ++a) vel[q + sv * a] = t[a];
+    for (int a = 0; a < 3; ++a) vel[q + sv * a] = t[a];
+  }
 }
 
 // p*m at one stencil point as an FP32 pair (hi exact product rounding, lo the
@@ -134,13 +140,13 @@ __global__ void __launch_bounds__(256) k_gen_cell(Geo g, Geo gq, MixedView M,
 
 int fst_mixedgen_pair(const Geo& g, const Geo& gq, const double* met, float* metf,
                       cudaStream_t st) {
-  k_metric_pair<<<cdiv(g.sv, 256), 256, 0, st>>>(g, gq, met, metf);
+  k_metric_pair<<<(unsigned)g.ngj * g.ngk, 128, 0, st>>>(g, gq, met, metf);
   return 1;
 }
 
 int fst_mixedgen_tvel(const Geo& g, const Geo& gq, const float* metf, float* vel,
                       cudaStream_t st) {
-  k_gen_tvel<<<cdiv(g.sv, 256), 256, 0, st>>>(g, gq, metf, vel);
+  k_gen_tvel<<<(unsigned)g.ngj * g.ngk, 128, 0, st>>>(gq, g.ngi, g.ngj, metf, vel);
   return 1;
 }
 

@@ -38,15 +38,28 @@ __global__ void __launch_bounds__(256) k_noise_maxabs(Geo g, const double* __res
                                                       unsigned long long* __restrict__ key) {
   const double* a = U + g.sv * cv;
   const int rows = g.ncj * (g.ndim == 3 ? g.nck : 1);
-  double mx = -1.7976931348623157e308;
-  for (int r = blockIdx.x; r < rows; r += gridDim.x) {  // one interior row per step
-    const int j = r % g.ncj, k = r / g.ncj;
-    const double* row = a + g.ng + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0);
+  // per-thread maximum on the integer key of |value| (an FP64 compare would
+  // run on the FP64 pipe); NaN skipped
+  unsigned long long kmx = FST_KEY_LOWEST;
+  constexpr int RB = 4;  // interior rows per step, their loads in flight together
+  for (int r0 = blockIdx.x * RB; r0 < rows; r0 += gridDim.x * RB)
     for (int i = threadIdx.x; i < g.nci; i += 256) {
-      const double s = fabs(row[i]);
-      if (s > mx) mx = s;
+      unsigned long long v[RB];
+#pragma unroll
+      for (int u = 0; u < RB; ++u) {  // a row past the end repeats the first one
+        const int r = r0 + u < rows ? r0 + u : 0, j = r % g.ncj, k = r / g.ncj;
+        v[u] = (unsigned long long)__double_as_longlong(
+                   a[g.ng + i + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]) &
+               0x7FFFFFFFFFFFFFFFull;
+      }
+#pragma unroll
+      for (int u = 0; u < RB; ++u)
+        if (v[u] <= 0x7FF0000000000000ull) {  // not NaN; |value| keys as value | sign bit
+          const unsigned long long key = v[u] | 0x8000000000000000ull;
+          kmx = key > kmx ? key : kmx;
+        }
     }
-  }
+  double mx = fst_unkey(kmx);
   mx = fst_warp_max(mx);
   __shared__ double sm[8];
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
@@ -488,7 +501,7 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
     cudaMemcpyAsync(key, &init, sizeof(init), cudaMemcpyHostToDevice, st);
     // 3D: maxCvar3D(var, 6), a fixed index (src/cart3d.cpp:346); 2D: C_hat
     const int cv = g.ndim == 3 ? 6 : g.nv + 1;
-    FST_LAUNCH(prof, "noise_max", st, n, k_noise_maxabs<<<4 * 152, 256, 0, st>>>(g, U, cv, key));
+    FST_LAUNCH(prof, "noise_max", st, n, k_noise_maxabs<<<8 * 152, 256, 0, st>>>(g, U, cv, key));
   }
   NoiseArgs A{};
   if (np.mode == 1 || g2)
