@@ -1,6 +1,6 @@
 // fst_oracle.cpp — CPU oracle for the FIESTA RHS + RK path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is judged
+// TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared
 // against; it is loaded by tests/, by __graft_entry__.smoke() and by the CPU
 // baseline leg of bench.py, and by nothing else.  It is never linked into the
 // product library.
