@@ -1153,7 +1153,9 @@ def export(path, prefix, height=None):
     ``<prefix>.cfg`` (the raw fst_config, read by fst::load_config in
     include/fst_module.hpp), ``<prefix>.U0`` (the initial state, LayoutLeft
     FP64), ``<prefix>.X`` (generalized and terrain grids: the node
-    coordinates) and ``<prefix>.json`` (a readable summary)."""
+    coordinates), ``<prefix>.noise`` (fiesta.noise on: the raw
+    fst_noise_params, read by fst::load_noise) and ``<prefix>.json`` (a
+    readable summary)."""
     import ctypes as C
     import json
 
@@ -1169,10 +1171,14 @@ def export(path, prefix, height=None):
     np.asfortranarray(U0).ravel(order="F").astype("<f8").tofile(prefix + ".U0")
     if X is not None:
         np.asfortranarray(X).ravel(order="F").astype("<f8").tofile(prefix + ".X")
+    noise = d.noise_params()
+    if noise is not None:
+        with open(prefix + ".noise", "wb") as f:
+            f.write(bytes(C.string_at(C.addressof(noise), C.sizeof(noise))))
     summary = {"deck": path, "title": d.title, "nt": d.nt, "dt": d.dt,
                "state_shape": list(abi.dims(cfg)), "grid": d.grid,
                "grid_shape": list(abi.grid_dims(cfg)) if X is not None else None,
-               "noise": d.noise_params() is not None, "config": abi.config_to_dict(cfg)}
+               "noise": noise is not None, "config": abi.config_to_dict(cfg)}
     with open(prefix + ".json", "w") as f:
         json.dump(summary, f, indent=1)
     return summary

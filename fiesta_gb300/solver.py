@@ -6,11 +6,11 @@ names and call order of the reference's ``rk_func`` subclasses
 (src/rkfunction.hpp:36-69, src/cart3d.cpp, src/cart2d.cpp) so that driver
 code written against them reads the same:
 
-    f = Cart3D(cfg)            # cart3d_func(cf)
+    f = Cart3D(cfg, noise=np_) # cart3d_func(cf); np_: fiesta.noise or None
     f.var = U0                 # loadInitialConditions
     f.preSim()
     for t in range(tstart, tend + 1):   # src/main.cpp:61, inclusive
-        f.preStep(); rkAdvance(cfg, f); f.postStep()
+        f.preStep(); rkAdvance(cfg, f); f.postStep()   # postStep: noise filter
 
 There is no CPU fallback: if libfst.so is missing or no GPU is present the
 constructor raises.
@@ -247,12 +247,13 @@ class _RkFunc:
 
     ndim = None
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, noise=None):
         if cfg.ndim != self.ndim:
             raise ValueError(f"{type(self).__name__} needs ndim={self.ndim}")
         self.cf = cfg
         self.solver = Solver(cfg)
         self.t = 0
+        self.noise = noise  # abi.FstNoiseParams of fiesta.noise, or None (off)
 
     # var / dvar / varx as in the reference (host copies)
     @property
@@ -280,6 +281,12 @@ class _RkFunc:
         pass  # folded into rkAdvance below (2D BCs run inside fst_rk_step)
 
     def postStep(self):
+        """The noise filter when fiesta.noise is on (src/cart3d.cpp:319-374,
+        src/cart2d.cpp:257-307, src/gen2d.cpp:150-179); the secondary
+        variables of an output step are ``varx``, read when writing."""
+        if self.noise is not None:
+            n = self.noise
+            self.solver.noise_filter(n.dh, n.eta, n.coff, n.nt, n.mode)
         self.t += 1
 
     def postSim(self):
@@ -287,10 +294,10 @@ class _RkFunc:
 
 
 class _CartFunc(_RkFunc):
-    def __init__(self, cfg):
+    def __init__(self, cfg, noise=None):
         if cfg.grid_type != abi.GRID_CARTESIAN:
             raise ValueError(f"{type(self).__name__} needs a cartesian grid (use Gen3D/Gen2D)")
-        super().__init__(cfg)
+        super().__init__(cfg, noise)
 
 
 class Cart3D(_CartFunc):
@@ -307,10 +314,10 @@ class _GenFunc(_RkFunc):
     module's view, preSim computes the metric tensor, and no step applies
     boundary conditions."""
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, noise=None):
         if cfg.grid_type != abi.GRID_GENERALIZED:
             raise ValueError(f"{type(self).__name__} needs grid_type = GRID_GENERALIZED")
-        super().__init__(cfg)
+        super().__init__(cfg, noise if cfg.ndim == 2 else None)  # gen3d: no noise filter
         self.grid = None
 
     def preSim(self):

@@ -80,7 +80,14 @@ class rk_func {
     check(fst_compute_rhs(ctx_, dvar.data(), dvar.size()), "compute");
   }
   virtual void preStep() {}   // 2D BCs run inside fst_rk_step
-  virtual void postStep() {}
+  // postStep's noise filter when the deck enables it (fiesta.noise, the
+  // `if (cf.noise)` block of src/cart3d.cpp:319-374, src/cart2d.cpp:257-307,
+  // src/gen2d.cpp:150-179).  The reference's other postStep work, the
+  // secondary variables of an output step, is secondary() here, called by
+  // the host when it writes.
+  virtual void postStep() {
+    if (noise_on_) check(fst_noise_filter(ctx_, &noise_), "postStep");
+  }
   virtual void preSim() {}
   virtual void postSim() { check(fst_synchronize(ctx_), "postSim"); }
 
@@ -89,6 +96,12 @@ class rk_func {
   void download() { check(fst_get_state(ctx_, var.data(), var.size()), "download"); }
   // Secondary variables (velocity, p, T, rho) of the device state into varx.
   void secondary() { check(fst_secondary(ctx_, varx.data(), varx.size()), "secondary"); }
+
+  // fiesta.noise.{dh, eta, coff, nt, mode} (src/input.cpp:270-277)
+  virtual void set_noise(const fst_noise_params& np) {
+    noise_ = np;
+    noise_on_ = true;
+  }
 
   fst_ctx* context() const { return ctx_; }
   const fst_config& config() const { return cf_; }
@@ -101,6 +114,8 @@ class rk_func {
   }
   fst_config cf_;
   fst_ctx* ctx_ = nullptr;
+  fst_noise_params noise_{};
+  bool noise_on_ = false;
 };
 
 class cart3d_func : public rk_func {
@@ -151,6 +166,8 @@ class gen3d_func : public gen_func {
   explicit gen3d_func(const fst_config& cf) : gen_func(cf) {
     if (cf.ndim != 3) throw Error(FST_ERR_INVALID, "gen3d_func needs ndim = 3");
   }
+  // gen3d_func::postStep has no noise filter (src/gen3d.cpp:111-128)
+  void set_noise(const fst_noise_params&) override {}
 };
 class gen2d_func : public gen_func {
  public:
@@ -182,6 +199,18 @@ inline void load_array(const std::string& path, HostArray& a) {
   const bool more = std::fgetc(f) != EOF;
   std::fclose(f);
   if (got != a.size() || more) throw Error(FST_ERR_SIZE, path + ": size does not match");
+}
+
+// <prefix>.noise, the raw fst_noise_params the deck exporter writes when
+// fiesta.noise.enabled is set; false when there is no such file.
+inline bool load_noise(const std::string& path, fst_noise_params& np) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  const size_t got = std::fread(&np, 1, sizeof(np), f);
+  const bool more = std::fgetc(f) != EOF;
+  std::fclose(f);
+  if (got != sizeof(np) || more) throw Error(FST_ERR_SIZE, path + " is not an fst_noise_params");
+  return true;
 }
 
 // The module src/main.cpp:40-50 picks for a config.

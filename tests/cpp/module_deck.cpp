@@ -1,6 +1,7 @@
 // Runs a deck exported by `python -m fiesta_gb300.deck <deck.lua> <prefix>`
 // through the C++ module interface: <prefix>.cfg, <prefix>.U0 (and .X for
-// generalized grids) in, <prefix>.U1 out after the given number of steps.
+// generalized grids, .noise when the deck enables the noise filter) in,
+// <prefix>.U1 out after the given number of steps.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -17,6 +18,8 @@ int main(int argc, char** argv) {
   try {
     const fst_config cf = fst::load_config(pre + ".cfg");
     auto f = fst::make_module(cf);
+    fst_noise_params np;
+    if (fst::load_noise(pre + ".noise", np)) f->set_noise(np);
     fst::load_array(pre + ".U0", f->var);
     if (auto* g = dynamic_cast<fst::gen_func*>(f.get())) fst::load_array(pre + ".X", g->grid);
     f->upload();

@@ -89,15 +89,41 @@ def test_deck_export_round_trip(tmp_path):
     assert summary["state_shape"] == list(abi.dims(cfg))
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("which", ["cart3d", "gen2d"])
-def test_gpu_cpp_runs_an_exported_deck(which, tmp_path):
-    """deck.lua -> python -m fiesta_gb300.deck -> C++ module interface ->
-    the same state as the oracle on the same inputs."""
+NOISE_KEYS = ("\nfiesta.noise.enabled = true\nfiesta.noise.dh = {dh}\nfiesta.noise.eta = 1e-3\n"
+              "fiesta.noise.coff = 0.05\n")
+
+
+def _deck_text(which, noise):
     from tests.test_deck import DECK_3D, DECK_GEN2D
     text = DECK_3D.replace('mode = "mixed"', 'mode = "plain"') if which == "cart3d" else DECK_GEN2D
+    if noise:  # postStep's noise filter after every step
+        text += NOISE_KEYS.format(dh=1e-5 if which == "cart3d" else 0.0)
+    return text
+
+
+def test_deck_export_writes_noise_params(tmp_path):
+    """fiesta.noise on: <prefix>.noise holds the raw fst_noise_params that
+    fst::load_noise reads; off: no such file."""
+    from fiesta_gb300 import deck
+    for noise in (False, True):
+        p = tmp_path / f"deck{int(noise)}.lua"
+        p.write_text(_deck_text("cart3d", noise))
+        pre = str(tmp_path / f"run{int(noise)}")
+        summary = deck.export(str(p), pre)
+        assert summary["noise"] is noise and os.path.exists(pre + ".noise") is noise
+    raw = open(pre + ".noise", "rb").read()
+    assert raw == bytes(deck.load(str(p)).noise_params())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which,noise", [("cart3d", False), ("gen2d", False), ("cart3d", True),
+                                         ("gen2d", True)])
+def test_gpu_cpp_runs_an_exported_deck(which, noise, tmp_path):
+    """deck.lua -> python -m fiesta_gb300.deck -> C++ module interface
+    (preStep, rkAdvance, postStep with the deck's noise filter) -> the same
+    state as the oracle on the same inputs."""
     p = tmp_path / "deck.lua"
-    p.write_text(text)
+    p.write_text(_deck_text(which, noise))
     prefix = str(tmp_path / "run")
     r = subprocess.run(["python", "-m", "fiesta_gb300.deck", str(p), prefix], cwd=ROOT,
                        capture_output=True, text=True)
@@ -113,5 +139,12 @@ def test_gpu_cpp_runs_an_exported_deck(which, tmp_path):
     o.set_state(U0)
     if cfg.grid_type == abi.GRID_GENERALIZED:
         o.set_grid(np.fromfile(prefix + ".X", dtype="<f8").reshape(abi.grid_dims(cfg), order="F"))
-    o.rk_step(2)
+    if noise:
+        from fiesta_gb300 import deck
+        np_ = deck.load(str(p)).noise_params()
+        for _ in range(2):
+            o.rk_step(1)
+            o.noise_filter(np_.dh, np_.eta, np_.coff, np_.nt, np_.mode)
+    else:
+        o.rk_step(2)
     assert same(U1, o.get_state())

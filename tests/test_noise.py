@@ -188,3 +188,27 @@ def test_gpu_sparse_noise_matches_oracle(case):
         assert _same_bits(s.get_state(), o.get_state())
     neg0 = _bits(U) == np.uint64(0x8000000000000000)
     assert (neg0 & (_bits(o.get_state()) == 0)).any()  # some -0 became +0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ndim", [3, 2])
+def test_gpu_module_postStep_runs_the_noise_filter(ndim):
+    """Cart3D / Cart2D with fiesta.noise on: preStep, rkAdvance, postStep
+    (the filter) per step, against the oracle's step + filter."""
+    from fiesta_gb300.solver import Cart2D, Cart3D, rkAdvance
+    cfg, U = _case(ndim, (10, 7, 6) if ndim == 3 else (19, 22), True, 11)
+    np_ = abi.FstNoiseParams(dh=1e-3, eta=0.1, coff=0.5, nt=1, mode=1)
+    f = (Cart3D if ndim == 3 else Cart2D)(cfg, noise=np_)
+    f.var = U
+    f.preSim()
+    o = Oracle(cfg)
+    o.set_state(U)
+    if ndim == 2:
+        o.apply_bcs()  # cart2d_func::preSim
+    for _ in range(2):
+        f.preStep()
+        rkAdvance(cfg, f)
+        f.postStep()
+        o.rk_step(1)
+        o.noise_filter(1e-3, 0.1, 0.5, 1, 1)
+    assert same(f.var, o.get_state())
