@@ -261,8 +261,7 @@ __global__ void __launch_bounds__(256) k_status(Geo g, StatusFields F,
 #pragma unroll
       for (int u = 0; u < RB; ++u) {
         const int r = r0 + u < rows ? r0 + u : 0, j = r % g.ncj, k = r / g.ncj;  // past the end: row 0
-        v[u] = (unsigned long long)__double_as_longlong(
-            a[g.ng + i + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]);
+        v[u] = fst_bits(a[g.ng + i + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]);
       }
 #pragma unroll
       for (int u = 0; u < RB; ++u) {

@@ -62,6 +62,16 @@ struct Phys {
   float dxmag_f, dxmag2_f, eps_f, kap_f, alpha_f, mu2d_f, kheat_f;
 };
 
+// The bit pattern of x through an opaque register move.  Integer tests on
+// the bits then stay integer tests: an optimiser may otherwise rewrite a
+// masked compare such as (bits & 0x7FF..F) >= c as an ordered FP compare
+// |x| >= c', which is false for NaN where the integer test is true.
+__device__ __forceinline__ unsigned long long fst_bits(double x) {
+  unsigned long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
+
 // --- order-preserving encoding of doubles for atomicMax -------------------
 __device__ __forceinline__ unsigned long long fst_key(double x) {
   unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -92,8 +102,7 @@ __device__ __forceinline__ double fst_warp_max(double v) {
 
 // finiteness from the exponent bits (integer ops, not the FP64 pipe)
 __device__ __forceinline__ bool fst_finite(double x) {
-  return ((unsigned long long)__double_as_longlong(x) & 0x7FF0000000000000ull) !=
-         0x7FF0000000000000ull;
+  return (fst_bits(x) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
 }
 
 // Linear index helpers

@@ -48,8 +48,7 @@ __global__ void __launch_bounds__(256) k_noise_maxabs(Geo g, const double* __res
 #pragma unroll
       for (int u = 0; u < RB; ++u) {  // a row past the end repeats the first one
         const int r = r0 + u < rows ? r0 + u : 0, j = r % g.ncj, k = r / g.ncj;
-        v[u] = (unsigned long long)__double_as_longlong(
-                   a[g.ng + i + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]) &
+        v[u] = fst_bits(a[g.ng + i + g.sy * (j + g.ng) + g.sz * (g.ndim == 3 ? k + g.ng : 0)]) &
                0x7FFFFFFFFFFFFFFFull;
       }
 #pragma unroll
@@ -129,7 +128,7 @@ __global__ void __launch_bounds__(256) k_noise_detect(Geo g, const double* __res
       for (int n = 0; n < 27; ++n) {
         const int pk = n / 9, rj = (n / 3) % 3, ci = n % 3;
         t[n] = var[(long long)(i - 1 + ci) + g.sy * (j + 1 - rj) + g.sz * (k + 1 - pk)];
-        emax = max(emax, (unsigned)(__double_as_longlong(t[n]) >> 52) & 0x7ffu);
+        emax = max(emax, (unsigned)(fst_bits(t[n]) >> 52) & 0x7ffu);
       }
       double sum = 2.0 * t[0];
       if (emax < 1023 + 1020) {
@@ -182,8 +181,8 @@ struct RemoveArgs {
 // magnitude and not -0: then each laplacian is finite, eta*D*0*lap is a
 // signed zero, and x + (+-0) == x bit for bit for every x but -0.
 __device__ __forceinline__ bool unsafe_value(double x, long long safe) {
-  const long long b = __double_as_longlong(x);
-  return (b & 0x7fffffffffffffffll) >= safe || b == (long long)0x8000000000000000ull;
+  const unsigned long long b = fst_bits(x);
+  return (b & 0x7fffffffffffffffull) >= (unsigned long long)safe || b == 0x8000000000000000ull;
 }
 
 // OR of `bits` over the block, written by thread 0 to *out
@@ -270,7 +269,7 @@ __global__ void __launch_bounds__(256) k_noise_tiles2(Geo g, const double* __res
 // mark the face neighbours for variable q -- later diagonals of this sweep
 // and, for the earlier ones, the next sweep
 __device__ __forceinline__ bool hard_value(double x, long long safe) {
-  return (__double_as_longlong(x) & 0x7fffffffffffffffll) >= safe;
+  return (fst_bits(x) & 0x7fffffffffffffffull) >= (unsigned long long)safe;
 }
 
 // cells of an 8-cube with x+y+z = s, ordered by z then y: those in plane z
@@ -279,182 +278,218 @@ __device__ __forceinline__ int row_cells(int u) {
   return u < 0 || u > 2 * T3 - 2 ? 0 : min(u, T3 - 1) - max(0, u - (T3 - 1)) + 1;
 }
 
-constexpr int R3 = 256;  // threads per 3D tile (a wavefront holds at most 48 cells)
+constexpr int R3 = 256;  // threads per 3D tile: up to three variables x 64 threads in a step
 
-// One diagonal (tx+ty+tz = diag) of 8x8x8 interior tiles, every filtered
-// variable in turn.  Inside a busy tile, wavefront w's cells go to
-// consecutive threads (a table in shared memory, built when first needed),
-// so the FP64 work of a step occupies ceil(cells/32) warps rather than
-// every warp the wavefront crosses.
-__global__ void __launch_bounds__(R3, 4) k_noise_remove3(Geo g, double* __restrict__ U,
+// OR of per-thread bits over the block into *acc (zeroed before a barrier)
+__device__ __forceinline__ void or_into(unsigned* acc, unsigned bits) {
+  const unsigned w = __reduce_or_sync(0xffffffffu, bits);
+  if ((threadIdx.x & 31) == 0 && w) atomicOr(acc, w);
+}
+
+// One diagonal (tx+ty+tz = diag) of 8x8x8 interior tiles.  The filtered
+// variables are swept side by side: threads 64q .. 64q+63 run variable q's
+// wavefront steps (each variable's sweep reads and writes only its own
+// values), with the cells of wavefront w in consecutive threads (a table in
+// shared memory), so a step's FP64 work occupies ceil(cells/32) warps per
+// variable rather than every warp the wavefront crosses.
+__global__ void __launch_bounds__(R3, 3) k_noise_remove3(Geo g, double* __restrict__ U,
                                                          const int* __restrict__ noise,
                                                          int* __restrict__ tiles, RemoveArgs R,
                                                          int diag, int ntx, int nty, int ntz) {
   const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx, tz = diag - tx - ty;
   if (tz < 0 || tz >= ntz) return;  // uniform over the block
   const int tile = blockIdx.x + ntx * nty * tz;
-  const int cand = tiles[tile];
+  const unsigned cand = (unsigned)tiles[tile];
   if (!cand) return;  // no variable to visit (k_noise_tiles3)
-  constexpr int E = T3 + 2, C = T3 * T3 * T3, W = 3 * T3 - 2, NL = (E * E * E + R3 - 1) / R3;
-  __shared__ double s[E][E][E];          // [z][y][x], tile + one-cell halo
+  constexpr int E = T3 + 2, C = T3 * T3 * T3, W = 3 * T3 - 2, E3 = E * E * E;
+  __shared__ double s[3][E][E][E];       // per variable: [z][y][x], tile + one-cell halo
   __shared__ int msk[C];                 // indicator of the tile's cells (0 outside)
   __shared__ unsigned short order[C];    // cells (x + 8y + 64z) by wavefront
   __shared__ short off[W + 1];           // wavefront w: order[off[w] .. off[w+1])
+  __shared__ unsigned busy_s, hard_s;
   const int tid = threadIdx.x;
   const int i0 = g.ng + T3 * tx - 1, j0 = g.ng + T3 * ty - 1, k0 = g.ng + T3 * tz - 1;
   const int xe = min(T3, g.ngi - g.ng - (i0 + 1)), ye = min(T3, g.ngj - g.ng - (j0 + 1)),
             ze = min(T3, g.ngk - g.ng - (k0 + 1));  // interior extent of the tile
+  if (tid == 0) busy_s = hard_s = 0;
+  unsigned bits = 0;
   for (int p = tid; p < C; p += R3) {
     const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
-    msk[p] = x < xe && y < ye && z < ze
-                 ? noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y) + g.sz * (k0 + 1 + z)]
-                 : 0;
+    const int m = x < xe && y < ye && z < ze
+                      ? noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y) + g.sz * (k0 + 1 + z)]
+                      : 0;
+    msk[p] = m;
+    bits |= (unsigned)m;
   }
-  const double D = R.dx * R.dx + R.dy * R.dy + R.dz * R.dz;
-  bool table = false;
   for (int q = 0; q < R.nvars; ++q) {
     if (!((cand >> q) & 1)) continue;
-    double* var = U + g.sv * pick(R.vars, q);
-    __syncthreads();  // msk is written; the previous variable's tile is stored
-    bool busy = false;
-    for (int p = tid; p < C; p += R3) busy = busy || ((msk[p] >> q) & 1);
+    const double* var = U + g.sv * pick(R.vars, q);
+    double* sq = &s[q][0][0][0];
+    constexpr int NL = (E3 + R3 - 1) / R3;
     double v[NL];
 #pragma unroll
     for (int u = 0; u < NL; ++u) {  // every load in flight before the first store
       const int p = tid + u * R3;
-      const int a = p % E, b = (p / E) % E, c = p / (E * E);
-      const int x = i0 + a, y = j0 + b, z = k0 + c;
-      if (p < E * E * E && x < g.ngi && y < g.ngj && z < g.ngk)
-        v[u] = var[(long long)x + g.sy * y + g.sz * z];
+      const int x = i0 + p % E, y = j0 + (p / E) % E, z = k0 + p / (E * E);
+      if (p < E3 && x < g.ngi && y < g.ngj && z < g.ngk) v[u] = var[(long long)x + g.sy * y + g.sz * z];
     }
 #pragma unroll
     for (int u = 0; u < NL; ++u) {
       const int p = tid + u * R3;
-      const int a = p % E, b = (p / E) % E, c = p / (E * E);
-      if (p < E * E * E && i0 + a < g.ngi && j0 + b < g.ngj && k0 + c < g.ngk) {
-        s[c][b][a] = v[u];
-        busy = busy || unsafe_value(v[u], R.safe);
+      const int x = i0 + p % E, y = j0 + (p / E) % E, z = k0 + p / (E * E);
+      if (p < E3 && x < g.ngi && y < g.ngj && z < g.ngk) {
+        sq[p] = v[u];
+        if (unsafe_value(v[u], R.safe)) bits |= 1u << q;
       }
     }
-    if (!__syncthreads_or(busy)) continue;
-    if (!table) {  // cells with x+y+z = w ordered by z then y
-      if (tid <= W) {
-        int o = 0;
-        for (int z = 0; z < T3; ++z)
-          for (int w = 0; w < tid; ++w) o += row_cells(w - z);
-        off[tid] = (short)o;
+  }
+  __syncthreads();  // busy_s zeroed
+  or_into(&busy_s, bits & cand & ((1u << R.nvars) - 1));
+  __syncthreads();
+  const unsigned busy = busy_s;
+  if (!busy) return;
+  if (tid <= W) {  // cells with x+y+z = w ordered by z then y
+    int o = 0;
+    for (int z = 0; z < T3; ++z)
+      for (int w = 0; w < tid; ++w) o += row_cells(w - z);
+    off[tid] = (short)o;
+  }
+  __syncthreads();
+  for (int p = tid; p < C; p += R3) {
+    const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3), w = x + y + z;
+    int r = off[w] + y - max(0, w - z - (T3 - 1));
+    for (int zz = 0; zz < z; ++zz) r += row_cells(w - zz);
+    order[r] = (unsigned short)p;
+  }
+  __syncthreads();
+  const double D = R.dx * R.dx + R.dy * R.dy + R.dz * R.dz;
+  const int q = tid >> 6, lt = tid & 63;  // this thread's variable and lane in its group
+  const bool mine = q < R.nvars && ((busy >> q) & 1);
+  for (int w = 0; w < W; ++w) {
+    const int t = off[w] + lt;
+    if (mine && t < off[w + 1]) {
+      const int p = order[t];
+      const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
+      if (x < xe && y < ye && z < ze) {
+        double (*sv3)[E][E] = s[q];
+        const int a = x + 1, b = y + 1, c = z + 1;
+        const double nz = (double)((msk[p] >> q) & 1);
+        const double lap = (sv3[c][b][a - 1] - 2 * sv3[c][b][a] + sv3[c][b][a + 1]) / (R.dx * R.dx) +
+                           (sv3[c][b - 1][a] - 2 * sv3[c][b][a] + sv3[c][b + 1][a]) / (R.dy * R.dy) +
+                           (sv3[c - 1][b][a] - 2 * sv3[c][b][a] + sv3[c + 1][b][a]) / (R.dz * R.dz);
+        const double dnoise = R.eta * D * nz * lap;
+        sv3[c][b][a] += dnoise;
       }
-      __syncthreads();
-      for (int p = tid; p < C; p += R3) {
-        const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3), w = x + y + z;
-        int r = off[w] + y - max(0, w - z - (T3 - 1));
-        for (int zz = 0; zz < z; ++zz) r += row_cells(w - zz);
-        order[r] = (unsigned short)p;
-      }
-      __syncthreads();
-      table = true;
     }
-    for (int w = 0; w < W; ++w) {
-      const int t = off[w] + tid;
-      if (t < off[w + 1]) {
-        const int p = order[t];
-        const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
-        if (x < xe && y < ye && z < ze) {
-          const int a = x + 1, b = y + 1, c = z + 1;
-          const double nz = (double)((msk[p] >> q) & 1);
-          const double lap = (s[c][b][a - 1] - 2 * s[c][b][a] + s[c][b][a + 1]) / (R.dx * R.dx) +
-                             (s[c][b - 1][a] - 2 * s[c][b][a] + s[c][b + 1][a]) / (R.dy * R.dy) +
-                             (s[c - 1][b][a] - 2 * s[c][b][a] + s[c + 1][b][a]) / (R.dz * R.dz);
-          const double dnoise = R.eta * D * nz * lap;
-          s[c][b][a] += dnoise;
-        }
-      }
-      __syncthreads();
-    }
-    bool hard = false;
+    __syncthreads();
+  }
+  unsigned hard = 0;
+  for (int qq = 0; qq < R.nvars; ++qq) {
+    if (!((busy >> qq) & 1)) continue;
+    double* var = U + g.sv * pick(R.vars, qq);
     for (int p = tid; p < C; p += R3) {
       const int x = p % T3, y = (p / T3) % T3, z = p / (T3 * T3);
       if (x < xe && y < ye && z < ze) {
-        const double val = s[z + 1][y + 1][x + 1];
+        const double val = s[qq][z + 1][y + 1][x + 1];
         var[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y) + g.sz * (k0 + 1 + z)] = val;
-        hard = hard || hard_value(val, R.safe);
+        if (hard_value(val, R.safe)) hard |= 1u << qq;
       }
     }
-    if (__syncthreads_or(hard) && tid < 6) {  // mark the face neighbours
-      const int ax = tid >> 1, d = (tid & 1) ? 1 : -1;
-      const int nx = tx + (ax == 0 ? d : 0), ny = ty + (ax == 1 ? d : 0), nz = tz + (ax == 2 ? d : 0);
-      if (nx >= 0 && nx < ntx && ny >= 0 && ny < nty && nz >= 0 && nz < ntz)
-        atomicOr(tiles + nx + ntx * (ny + nty * nz), 1 << q);
-    }
+  }
+  or_into(&hard_s, hard);
+  __syncthreads();
+  const unsigned hb = hard_s;
+  if (hb && tid < 6) {  // mark the face neighbours for the variables left unsafe
+    const int ax = tid >> 1, d = (tid & 1) ? 1 : -1;
+    const int nx = tx + (ax == 0 ? d : 0), ny = ty + (ax == 1 ? d : 0), nz = tz + (ax == 2 ? d : 0);
+    if (nx >= 0 && nx < ntx && ny >= 0 && ny < nty && nz >= 0 && nz < ntz)
+      atomicOr(tiles + nx + ntx * (ny + nty * nz), (int)hb);
   }
 }
 
-// One diagonal (tx+ty = diag) of 32x32 interior tiles, one warp each, every
-// filtered variable in turn: lane t takes the t-th cell of wavefront w.
-__global__ void __launch_bounds__(32) k_noise_remove2(Geo g, double* __restrict__ U,
+// One diagonal (tx+ty = diag) of 32x32 interior tiles, one warp per filtered
+// variable (at most two in 2D), swept side by side: lane t of warp q takes
+// the t-th cell of variable q's wavefront w.
+__global__ void __launch_bounds__(64) k_noise_remove2(Geo g, double* __restrict__ U,
                                                       const int* __restrict__ noise,
                                                       int* __restrict__ tiles, RemoveArgs R,
                                                       int diag, int ntx, int nty) {
   const int tx = blockIdx.x, ty = diag - tx;
   if (ty < 0 || ty >= nty) return;
-  const int cand = tiles[tx + ntx * ty];
+  const unsigned cand = (unsigned)tiles[tx + ntx * ty];
   if (!cand) return;  // no variable to visit (k_noise_tiles2)
   constexpr int E = T2 + 2;
-  __shared__ double s[E][E];  // [y][x]
+  __shared__ double s[2][E][E];  // per variable: [y][x]
   __shared__ int msk[T2 * T2];
+  __shared__ unsigned busy_s, hard_s;
   const int tid = threadIdx.x;
   const int i0 = g.ng + T2 * tx - 1, j0 = g.ng + T2 * ty - 1;
   const int xe = min(T2, g.ngi - g.ng - (i0 + 1)), ye = min(T2, g.ngj - g.ng - (j0 + 1));
-  for (int p = tid; p < T2 * T2; p += 32) {
+  if (tid == 0) busy_s = hard_s = 0;
+  unsigned bits = 0;
+  for (int p = tid; p < T2 * T2; p += 64) {
     const int x = p % T2, y = p / T2;
-    msk[p] = x < xe && y < ye ? noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y)] : 0;
+    const int m = x < xe && y < ye ? noise[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y)] : 0;
+    msk[p] = m;
+    bits |= (unsigned)m;
   }
-  const double dx = R.dx, dy = R.dy;
-  const double D = dx * dx + dy * dy;
   for (int q = 0; q < R.nvars; ++q) {
     if (!((cand >> q) & 1)) continue;
-    double* var = U + g.sv * pick(R.vars, q);
-    bool busy = false;
-    __syncthreads();
-    for (int p = tid; p < T2 * T2; p += 32) busy = busy || ((msk[p] >> q) & 1);
-    for (int p = tid; p < E * E; p += 32) {
+    const double* var = U + g.sv * pick(R.vars, q);
+    for (int p = tid; p < E * E; p += 64) {
       const int a = p % E, b = p / E;
       const int x = i0 + a, y = j0 + b;
       if (x < g.ngi && y < g.ngj) {
         const double val = var[(long long)x + g.sy * y];
-        s[b][a] = val;
-        busy = busy || unsafe_value(val, R.safe);
+        s[q][b][a] = val;
+        if (unsafe_value(val, R.safe)) bits |= 1u << q;
       }
     }
-    if (!__syncthreads_or(busy)) continue;
-    for (int w = 0; w < 2 * T2 - 1; ++w) {
-      const int y = max(0, w - (T2 - 1)) + tid, x = w - y;  // x >= 0 while y <= w
-      if (x >= 0 && y < ye && x < xe) {
-        const int a = x + 1, b = y + 1;
-        const double nz = (double)((msk[x + T2 * y] >> q) & 1);
-        const double lgrad = (s[b][a] - s[b][a - 1]) / dx;
-        const double rgrad = (s[b][a + 1] - s[b][a]) / dx;
-        const double bgrad = (s[b][a] - s[b - 1][a]) / dy;
-        const double tgrad = (s[b + 1][a] - s[b][a]) / dy;
-        const double dv = R.eta * D * nz * ((rgrad - lgrad) / dx + (tgrad - bgrad) / dy);
-        s[b][a] += dv;
-      }
-      __syncwarp();
+  }
+  __syncthreads();
+  or_into(&busy_s, bits & cand & ((1u << R.nvars) - 1));
+  __syncthreads();
+  const unsigned busy = busy_s;
+  if (!busy) return;
+  const double dx = R.dx, dy = R.dy;
+  const double D = dx * dx + dy * dy;
+  const int q = tid >> 5, lt = tid & 31;
+  const bool mine = q < R.nvars && ((busy >> q) & 1);
+  for (int w = 0; w < 2 * T2 - 1; ++w) {
+    const int y = max(0, w - (T2 - 1)) + lt, x = w - y;  // x >= 0 while y <= w
+    if (mine && x >= 0 && y < ye && x < xe) {
+      const int a = x + 1, b = y + 1;
+      const double nz = (double)((msk[x + T2 * y] >> q) & 1);
+      const double lgrad = (s[q][b][a] - s[q][b][a - 1]) / dx;
+      const double rgrad = (s[q][b][a + 1] - s[q][b][a]) / dx;
+      const double bgrad = (s[q][b][a] - s[q][b - 1][a]) / dy;
+      const double tgrad = (s[q][b + 1][a] - s[q][b][a]) / dy;
+      const double dv = R.eta * D * nz * ((rgrad - lgrad) / dx + (tgrad - bgrad) / dy);
+      s[q][b][a] += dv;
     }
-    bool hard = false;
-    for (int p = tid; p < T2 * T2; p += 32) {
+    __syncwarp();  // each variable's steps stay within its own warp
+  }
+  __syncthreads();
+  unsigned hard = 0;
+  for (int qq = 0; qq < R.nvars; ++qq) {
+    if (!((busy >> qq) & 1)) continue;
+    double* var = U + g.sv * pick(R.vars, qq);
+    for (int p = tid; p < T2 * T2; p += 64) {
       const int x = p % T2, y = p / T2;
       if (x < xe && y < ye) {
-        const double val = s[y + 1][x + 1];
+        const double val = s[qq][y + 1][x + 1];
         var[(long long)(i0 + 1 + x) + g.sy * (j0 + 1 + y)] = val;
-        hard = hard || hard_value(val, R.safe);
+        if (hard_value(val, R.safe)) hard |= 1u << qq;
       }
     }
-    if (__syncthreads_or(hard) && tid < 4) {  // mark the face neighbours
-      const int d = (tid & 1) ? 1 : -1;
-      const int nx = tx + (tid < 2 ? d : 0), ny = ty + (tid < 2 ? 0 : d);
-      if (nx >= 0 && nx < ntx && ny >= 0 && ny < nty) atomicOr(tiles + nx + ntx * ny, 1 << q);
-    }
+  }
+  or_into(&hard_s, hard);
+  __syncthreads();
+  const unsigned hb = hard_s;
+  if (hb && tid < 4) {  // mark the face neighbours
+    const int d = (tid & 1) ? 1 : -1;
+    const int nx = tx + (tid < 2 ? d : 0), ny = ty + (tid < 2 ? 0 : d);
+    if (nx >= 0 && nx < ntx && ny >= 0 && ny < nty) atomicOr(tiles + nx + ntx * ny, (int)hb);
   }
 }
 
@@ -550,7 +585,7 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
       for (int tau = 0; tau < np.nt; ++tau)
         for (int d = 0; d <= ntx + nty - 2; ++d)
           FST_LAUNCH(prof, "noise_remove", st, n,
-                     k_noise_remove2<<<ntx, 32, 0, st>>>(g, U, noise, tiles, R, d, ntx, nty));
+                     k_noise_remove2<<<ntx, 64, 0, st>>>(g, U, noise, tiles, R, d, ntx, nty));
     }
   }
   return n;
