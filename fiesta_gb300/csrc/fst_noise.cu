@@ -14,12 +14,14 @@
 // place, in loop order (i slowest): a cell sees its -x, -y, -z neighbours
 // already updated and its +x, +y, +z neighbours not yet.  The same holds
 // for a sweep by wavefronts i+j+k = const, which k_noise_remove runs tile by
-// tile: one launch per diagonal of 8x8x8 (2D: 16x16) tiles, and inside a
+// tile: one launch per diagonal of 8x8x8 (2D: 32x32) tiles, and inside a
 // tile one step per cell wavefront on a shared-memory copy with a one-cell
-// halo (tiles on one diagonal share no face).  One launch sweeps every
-// filtered variable (each sweep reads and writes its own variable only), and
-// a tile without a flagged cell whose values make the update a provable
-// no-op skips the wavefront (the FP64 steps are the cost on this part).
+// halo (tiles on one diagonal share no face).  Each tile sweeps every
+// filtered variable side by side (each sweep reads and writes its own
+// variable only).  A tile without a flagged cell whose values make the
+// update a provable no-op skips its wavefronts, and k_noise_tiles marks in
+// one launch the tiles that cannot skip, so the others return at once (the
+// FP64 steps are the cost on this part).
 //
 // Built with --fmad=false; expressions keep the reference's operation order.
 #include <cmath>
