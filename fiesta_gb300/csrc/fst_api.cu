@@ -53,6 +53,7 @@ struct fst_ctx {
   unsigned long long* dstat = nullptr;  // fst_status keys
   int* dnoise = nullptr;                 // noise indicator (fst_noise_filter)
   unsigned long long* dnoise_key = nullptr;
+  NoiseGraph noise_graph;                // the filter's sweeps as a CUDA graph
   fst_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
@@ -492,6 +493,7 @@ void fst_destroy(fst_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
   fst_mixed3d_release(c->bm);
+  fst_noise_graph_release(c->noise_graph);
   if (c->Rdev) cudaFree(c->Rdev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -754,7 +756,8 @@ int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
     if (e != cudaSuccess) return cuda_fail(c, e, "noise init");
   }
   c->stats.kernel_launches +=
-      fst_noise_launch(g, c->cf, c->Ua, c->dnoise, c->dnoise_key, *np, c->stream, &c->prof);
+      fst_noise_launch(g, c->cf, c->Ua, c->dnoise, c->dnoise_key, *np, c->stream, &c->prof,
+                       &c->noise_graph);
   return check_launch(c, "noise filter");
 }
 

@@ -178,11 +178,21 @@ int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const Mix
                     const double* U, cudaStream_t st);
 
 // fst_noise.cu: the postStep noise filter on state U; `noise` holds
-// fst_noise_ints(g) ints (the indicator, then the removal's tile marks)
+// fst_noise_ints(g) ints (the indicator, then the removal's tile marks).
+// The tile marks and removal sweeps (about a hundred short launches) run as
+// a CUDA graph, captured on a private stream at the first unprofiled call
+// and replayed while their launch parameters stay the same.
+struct NoiseGraph {
+  cudaStream_t cap = nullptr;  // capture stream (the caller's may be the legacy stream)
+  cudaGraphExec_t exec = nullptr;
+  unsigned char sig[128] = {};
+  int launches = 0;
+};
+void fst_noise_graph_release(NoiseGraph& ng);
 long long fst_noise_ints(const Geo& g);
 int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
                      unsigned long long* key, const fst_noise_params& np, cudaStream_t st,
-                     Prof* prof);
+                     Prof* prof, NoiseGraph* graph);
 
 // fst_mixed3d.cu: the 3D mixed/hybrid right-hand side + RK stage (two
 // fused kernels fed by TMA plane loads) and its tensor maps

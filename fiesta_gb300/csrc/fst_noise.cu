@@ -519,9 +519,15 @@ long long fst_noise_ints(const Geo& g) {
   return g.sv + tiles;
 }
 
+void fst_noise_graph_release(NoiseGraph& ng) {
+  if (ng.exec) cudaGraphExecDestroy(ng.exec);
+  if (ng.cap) cudaStreamDestroy(ng.cap);
+  ng = NoiseGraph{};
+}
+
 int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
                      unsigned long long* key, const fst_noise_params& np, cudaStream_t st,
-                     Prof* prof) {
+                     Prof* prof, NoiseGraph* graph) {
   int n = 0;
   // largest lattice index per axis (src/cart3d.cpp:326-339, src/cart2d.cpp:262-272);
   // gen2d_func::postStep (src/gen2d.cpp:150-179) counts from nci - 1, visits
@@ -571,24 +577,68 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
   RemoveArgs R{A.nvars, {A.vars[0], A.vars[1], A.vars[2]}, np.eta, dx, dy, dz,
                skip_bound(np.eta, dx, dy, g.ndim == 3 ? dz : dy)};
   int* tiles = noise + g.sv;  // candidate tiles (fst_noise_ints)
-  if (np.nt > 0) {
+  // the tile marks, then nt sweeps of one launch per tile diagonal
+  auto sweeps = [&](cudaStream_t s, Prof* pr) {
+    int L = 0;
     if (g.ndim == 3) {
       const int ntx = (g.nci + T3 - 1) / T3, nty = (g.ncj + T3 - 1) / T3, ntz = (g.nck + T3 - 1) / T3;
-      FST_LAUNCH(prof, "noise_tiles", st, n,
-                 k_noise_tiles3<<<ntx * nty * ntz, 256, 0, st>>>(g, U, noise, tiles, R, ntx, nty));
+      FST_LAUNCH(pr, "noise_tiles", s, L,
+                 k_noise_tiles3<<<ntx * nty * ntz, 256, 0, s>>>(g, U, noise, tiles, R, ntx, nty));
       for (int tau = 0; tau < np.nt; ++tau)
         for (int d = 0; d <= ntx + nty + ntz - 3; ++d)
-          FST_LAUNCH(prof, "noise_remove", st, n,
-                     k_noise_remove3<<<ntx * nty, R3, 0, st>>>(g, U, noise, tiles, R, d, ntx, nty, ntz));
+          FST_LAUNCH(pr, "noise_remove", s, L,
+                     k_noise_remove3<<<ntx * nty, R3, 0, s>>>(g, U, noise, tiles, R, d, ntx, nty, ntz));
     } else {
       const int ntx = (g.nci + T2 - 1) / T2, nty = (g.ncj + T2 - 1) / T2;
-      FST_LAUNCH(prof, "noise_tiles", st, n,
-                 k_noise_tiles2<<<ntx * nty, 256, 0, st>>>(g, U, noise, tiles, R, ntx));
+      FST_LAUNCH(pr, "noise_tiles", s, L,
+                 k_noise_tiles2<<<ntx * nty, 256, 0, s>>>(g, U, noise, tiles, R, ntx));
       for (int tau = 0; tau < np.nt; ++tau)
         for (int d = 0; d <= ntx + nty - 2; ++d)
-          FST_LAUNCH(prof, "noise_remove", st, n,
-                     k_noise_remove2<<<ntx, 64, 0, st>>>(g, U, noise, tiles, R, d, ntx, nty));
+          FST_LAUNCH(pr, "noise_remove", s, L,
+                     k_noise_remove2<<<ntx, 64, 0, s>>>(g, U, noise, tiles, R, d, ntx, nty));
     }
+    return L;
+  };
+  if (np.nt <= 0) return n;
+  if (!graph || (prof && prof->on)) return n + sweeps(st, prof);  // per-kernel timing
+  // the launch parameters the graph bakes in
+  struct Sig {
+    const double* U;
+    const int* noise;
+    RemoveArgs R;
+    int nt, ndim, nci, ncj, nck;
+  } sig;
+  memset(&sig, 0, sizeof(sig));
+  sig.U = U;
+  sig.noise = noise;
+  sig.R = R;
+  sig.nt = np.nt;
+  sig.ndim = g.ndim;
+  sig.nci = g.nci;
+  sig.ncj = g.ncj;
+  sig.nck = g.nck;
+  static_assert(sizeof(Sig) <= sizeof(graph->sig), "noise graph signature");
+  if (!graph->exec || memcmp(graph->sig, &sig, sizeof(sig)) != 0) {
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    graph->exec = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!graph->cap) e = cudaStreamCreateWithFlags(&graph->cap, cudaStreamNonBlocking);
+    cudaGraph_t gr = nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(graph->cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      graph->launches = sweeps(graph->cap, nullptr);
+      e = cudaStreamEndCapture(graph->cap, &gr);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&graph->exec, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    if (e != cudaSuccess) {  // no graph on this setup: launch the sweeps directly
+      if (graph->exec) cudaGraphExecDestroy(graph->exec);
+      graph->exec = nullptr;
+      cudaGetLastError();
+      return n + sweeps(st, prof);
+    }
+    memcpy(graph->sig, &sig, sizeof(sig));
   }
-  return n;
+  cudaGraphLaunch(graph->exec, st);
+  return n + graph->launches;
 }
