@@ -72,13 +72,6 @@ __global__ void __launch_bounds__(256) k_noise_maxabs(Geo g, const double* __res
   }
 }
 
-// the largest lattice centre offset (0, 2, .., 2*Mx) whose 3-wide block
-// covers cell offset o (o in [-1, 2*Mx+1])
-__device__ __forceinline__ int last_centre(int o, int Mx) {
-  if ((o & 1) == 0) return o;
-  return o + 1 <= 2 * Mx ? o + 1 : o - 1;
-}
-
 // the filtered variables and the detection constants, computed on the host
 // with the reference's expressions (products and quotients only, so IEEE
 // rounding makes them the same there as on the device)
