@@ -277,6 +277,11 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
                 "algorithmic_bytes_per_launch": b, "avg_launch_ms": per_ms,
                 "peak_source": peak_kind,
                 "share_of_step": tot / ms}
+        if mode_name == "plain":  # the FP64 pipe, not HBM, is this kernel's roof
+            roof["bound"] = "fp64"
+            roof["bound_note"] = ("FP64 pipe 85 % busy, DRAM a few % (ncu, "
+                                  "profiles/flux3d_plain_64cubed.md); the GB/s figures show how "
+                                  "far below the HBM roof an FP64-bound kernel sits")
 
     # end to end through the C ABI with host buffers: upload, step, download
     n_state = int(np.prod(abi.dims(cfg)))
