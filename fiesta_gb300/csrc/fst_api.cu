@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256) k_status(Geo g, StatusFields F,
   // would run on the FP64 pipe, two per value; NaN is skipped, as by the
   // reference's `if (v > max)` reducers
   unsigned long long kmx = FST_KEY_LOWEST, kmn = 0xFFEFFFFFFFFFFFFFull;  // keys of -+DBL_MAX
-  constexpr int RB = 4;  // interior rows per step, their loads in flight together
+  constexpr int RB = 8;  // interior rows per step, their loads in flight together
   for (int r0 = blockIdx.x * RB; r0 < rows; r0 += gridDim.x * RB)
     for (int i = threadIdx.x; i < g.nci; i += 256) {
       unsigned long long v[RB];
