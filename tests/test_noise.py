@@ -212,3 +212,25 @@ def test_gpu_module_postStep_runs_the_noise_filter(ndim):
         o.rk_step(1)
         o.noise_filter(1e-3, 0.1, 0.5, 1, 1)
     assert same(f.var, o.get_state())
+
+
+@pytest.mark.gpu
+def test_gpu_noise_graph_follows_parameter_changes():
+    """The sweeps replay as a captured CUDA graph; a call with other
+    parameters (eta, nt, mode, cutoff) must re-capture, and a profiled call
+    (kernels launched one by one) must give the same bits."""
+    from fiesta_gb300.solver import Solver
+    cfg, U = _case(3, (19, 17, 10), True, 12)
+    calls = [(1e-3, 0.1, 0.5, 1, 1), (1e-3, 0.1, 0.5, 1, 1), (1e-3, 0.2, 0.5, 1, 1),
+             (1e-3, 0.2, 0.5, 2, 1), (5e-4, 0.2, 0.0, 2, 2), (1e-3, 0.1, 0.5, 1, 1)]
+    o, s, p = Oracle(cfg), Solver(cfg), Solver(cfg)
+    for x in (o, s, p):
+        x.set_state(U)
+    p.set_profiling(True)
+    for args in calls:
+        o.noise_filter(*args)
+        s.noise_filter(*args)
+        p.noise_filter(*args)
+        assert _same_bits(s.get_state(), o.get_state()), args
+        assert _same_bits(p.get_state(), o.get_state()), args
+    assert any(k.startswith("noise_remove") for k in p.kernel_times())
