@@ -34,7 +34,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mcell-steps/s 256^3 5-species viscous RK2 (FP64 plain / mixed / hybrid)"
-WORKLOAD = "3D five-species viscous mixing, C-equation on, 256^3 interior, outflow BCs"
+def workload(n=256):
+    return f"3D five-species viscous mixing, C-equation on, {n}^3 interior, outflow BCs"
+
 SPECIES = [dict(gamma=g, M=m / 1000.0, mu=mu) for g, m, mu in
            zip([1.4, 1.67, 1.3, 1.32, 1.4], [28.96, 4.0, 44.0, 16.0, 2.0],
                [1.8e-5, 1.99e-5, 1.47e-5, 1.1e-5, 0.88e-5])]
@@ -634,7 +636,7 @@ def main():
                 "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
                 "ms_per_step": (a.cpu_sample ** 3) / (val * 1e6) * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": WORKLOAD, "grid": [a.size] * 3,
+                "data": "synthetic", "config": {"workload": workload(a.size), "grid": [a.size] * 3,
                                                 "species": 5, "sample_grid": [a.cpu_sample] * 3},
                 "cpu_baseline": cb,
                 "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
@@ -707,10 +709,11 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if head == "plain" else "f32+f64",
         "data": "synthetic (seeded compiled IC generator: 8 Gaussian pressure kernels, 5 species)",
-        "config": {"workload": WORKLOAD, "grid": [n] * 3, "species": 5, "nvt": 14,
+        "config": {"workload": workload(n), "grid": [n] * 3, "species": 5, "nvt": 14,
                    "mode": head, "headline_rule": "fastest mode with every conserved field "
                    "within rel-L2 1e-5 of the FP64 path after warmup+steps steps",
-                   "dt": dt, "l2": "state 2.0 GB > L2 (no flush needed)",
+                   "dt": dt, "l2": f"state {(n + 6) ** 3 * 14 * 8 / 1e9:.2f} GB "
+                   f"{'>' if (n + 6) ** 3 * 14 * 8 > 129e6 else '<'} L2 (129 MB)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": r["roofline"],
         # whole-step figure: the compulsory FP64 state traffic of a fused
