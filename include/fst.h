@@ -226,7 +226,10 @@ typedef struct fst_noise_params {
  * for bit.  The noise indicator persists between calls, as the module's
  * member array does.  On a generalized 2D grid it is gen2d_func's variant
  * (src/gen2d.cpp:150-179: lattice from nci - 1, no cutoff, both momenta);
- * the generalized 3D module has none (FST_ERR_UNSUPPORTED). */
+ * the generalized 3D module has none (FST_ERR_UNSUPPORTED).  The first call
+ * with profiling off captures the removal sweeps into a CUDA graph on a
+ * private stream (make it outside any stream capture of the caller); later
+ * calls with the same parameters replay it. */
 int fst_noise_filter(fst_ctx* ctx, const fst_noise_params* np);
 
 /* Node coordinates of a generalized grid: (ni, nj, nk, 3) doubles, LayoutLeft,
