@@ -44,7 +44,18 @@ __global__ void k_face(Geo g, double* __restrict__ U, int axis, int side, int ty
 
 inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
+// Reset n reduction words to v on the stream (in place of a copy from host
+// memory, so that the reset is an ordinary stream-ordered kernel).
+__global__ void k_fill_keys(unsigned long long* __restrict__ p, int n, unsigned long long v) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) p[t] = v;
+}
+
 }  // namespace
+
+void fst_fill_keys(unsigned long long* p, int n, unsigned long long v, cudaStream_t st) {
+  if (n > 0) k_fill_keys<<<nblk(n, 64), 64, 0, st>>>(p, n, v);
+}
 
 // Host launcher: the whole applyBCs sequence on `stream`.  Returns the number
 // of kernels launched.

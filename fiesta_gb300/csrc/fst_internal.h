@@ -73,6 +73,8 @@ int fst_mixedgen_cell(const Geo& g, const Geo& gq, const MixedView& M, const flo
                       cudaStream_t st);
 
 // fst_bc.cu
+// n words of p set to v by a kernel on st (reduction-word resets)
+void fst_fill_keys(unsigned long long* p, int n, unsigned long long v, cudaStream_t st);
 int fst_launch_bcs(const Geo& g, const fst_config& cf, double* U, cudaStream_t stream, Prof* prof);
 
 // fst_plain3d.cu

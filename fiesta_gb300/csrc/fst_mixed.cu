@@ -189,8 +189,7 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
                     bool ghosts, cudaStream_t st, Prof* prof) {
   int n = 0;
   if (P.ceq) {
-    const unsigned long long init[2] = {FST_KEY_LOWEST, FST_KEY_LOWEST};
-    cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
   }
   const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.mu32, b.nrg, b.C, b.T32, b.rho64, b.p32};
   if (g.ndim == 3) {

@@ -18,6 +18,19 @@ namespace {
 constexpr size_t kScratchDoubles = FST_NOALLOC_SCRATCH_BYTES / sizeof(double);
 static __device__ __align__(256) double g_scratch[kScratchDoubles];
 
+// Work doubles per cell: rho, p, u, v, T, e (6), the face fluxes (2 nv),
+// with viscosity the stress (6) and heat flux (2), with the C-equation the
+// face tensors (8); plus two reduction words per call.
+constexpr size_t work_per_cell(int nv, bool visc, bool ceq) {
+  return 6 + 2 * (size_t)nv + (visc ? 8 : 0) + (ceq ? 8 : 0);
+}
+// The largest 2D mixture (nv = 3 + FST_MAX_SPECIES, viscous, C-equation) on
+// the largest accepted grid fits the array, so the cell count is the only
+// limit a caller meets.
+static_assert((size_t)FST_NOALLOC_MAX_CELLS * work_per_cell(3 + FST_MAX_SPECIES, true, true) + 2 <=
+                  kScratchDoubles,
+              "the fixed scratch array must hold the largest accepted 2D grid");
+
 constexpr int kMaxDevices = 64;
 std::mutex g_lock;
 double* g_addr[kMaxDevices] = {nullptr};
@@ -30,7 +43,11 @@ int scratch_address(double** out) {
     std::fprintf(stderr, "fst_rhs2d_noalloc: cudaGetDevice: %s\n", cudaGetErrorString(e));
     return FST_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) return FST_ERR_UNSUPPORTED;
+  if (dev < 0 || dev >= kMaxDevices) {
+    std::fprintf(stderr, "fst_rhs2d_noalloc: device index %d is beyond the %d supported\n", dev,
+                 kMaxDevices);
+    return FST_ERR_UNSUPPORTED;
+  }
   std::lock_guard<std::mutex> guard(g_lock);
   if (!g_addr[dev]) {
     void* p = nullptr;
@@ -50,6 +67,14 @@ int scratch_address(double** out) {
 extern "C" int fst_rhs2d_noalloc(const fst_config* cfg, const double* d_U, double* d_R, size_t n,
                                  void* cuda_stream) {
   if (!cfg || !d_U || !d_R) return FST_ERR_INVALID;
+  // An error left pending by the caller's own earlier work is reported as
+  // such and left in place, so that a launch failure below is ours alone.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "fst_rhs2d_noalloc: a CUDA error from earlier work is pending: %s\n",
+                 cudaGetErrorString(e));
+    return FST_ERR_CUDA;
+  }
   Geo g;
   Phys P;
   const std::string why = fst_setup_geo_phys(cfg, g, P);
@@ -63,15 +88,12 @@ extern "C" int fst_rhs2d_noalloc(const fst_config* cfg, const double* d_U, doubl
   }
   const size_t cells = (size_t)g.sv;
   if (n != cells * (size_t)g.nvt) return FST_ERR_SIZE;
-  // work arrays: rho, p, u, v, T, e, fluxes (2 nv), stress (6), heat flux (2),
-  // C-equation tensors (8), two reduction words
-  const size_t per_cell = 6 + 2 * (size_t)g.nv + (cfg->visc ? 8 : 0) + (cfg->ceq ? 8 : 0);
-  const size_t need = cells * per_cell + 2;
+  const size_t need = cells * work_per_cell(g.nv, cfg->visc != 0, cfg->ceq != 0) + 2;
   if (cells > FST_NOALLOC_MAX_CELLS || need > kScratchDoubles) {
     std::fprintf(stderr,
-                 "fst_rhs2d_noalloc: grid of %zu cells (with ghosts) exceeds the fixed "
-                 "scratch limit of %d cells\n",
-                 cells, FST_NOALLOC_MAX_CELLS);
+                 "fst_rhs2d_noalloc: grid of %zu cells (with ghosts) needs %zu work doubles; "
+                 "the limits are %d cells and %zu doubles\n",
+                 cells, need, FST_NOALLOC_MAX_CELLS, kScratchDoubles);
     return FST_ERR_SIZE;
   }
   double* base = nullptr;
@@ -101,7 +123,7 @@ extern "C" int fst_rhs2d_noalloc(const fst_config* cfg, const double* d_U, doubl
 
   // the right-hand side is zero outside the interior, like the reference's
   // zero-initialised dvar; the interior is overwritten below
-  cudaError_t e = cudaMemsetAsync(d_R, 0, n * sizeof(double), st);
+  e = cudaMemsetAsync(d_R, 0, n * sizeof(double), st);
   if (e != cudaSuccess) {
     std::fprintf(stderr, "fst_rhs2d_noalloc: cudaMemsetAsync: %s\n", cudaGetErrorString(e));
     return FST_ERR_CUDA;

@@ -533,8 +533,7 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
   const int L = (g.nck + 1) % 2 == 0 ? (g.nck + 1) / 2 : g.nck / 2;
   const bool ceq = cf.ceq != 0 && !g2;
   if (ceq) {
-    const unsigned long long init = FST_KEY_LOWEST;
-    cudaMemcpyAsync(key, &init, sizeof(init), cudaMemcpyHostToDevice, st);
+    fst_fill_keys(key, 1, FST_KEY_LOWEST, st);
     // 3D: maxCvar3D(var, 6), a fixed index (src/cart3d.cpp:346); 2D: C_hat
     const int cv = g.ndim == 3 ? 6 : g.nv + 1;
     FST_LAUNCH(prof, "noise_max", st, n, k_noise_maxabs<<<8 * 152, 256, 0, st>>>(g, U, cv, key));

@@ -443,8 +443,7 @@ int fst_plain3d_stage(const Geo& g, const Phys& P, const Plain3DBufs& b, const d
                       cudaStream_t st, Prof* prof) {
   int n = 0;
   if (P.ceq) {
-    const unsigned long long init[2] = {FST_KEY_LOWEST, FST_KEY_LOWEST};
-    cudaMemcpyAsync(b.red, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
   }
   FST_LAUNCH(prof, "prim3d", st, n,
              k_prim3d<<<cdiv(g.sv, 256), 256, 0, st>>>(g, P, Uin, b.rho, b.pr, b.vel,

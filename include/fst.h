@@ -277,9 +277,15 @@ int fst_kernel_times(fst_ctx* ctx, fst_kernel_time* out, int max, int* count);
  * into device memory d_R (same layout; zero outside the interior), on
  * `cuda_stream` (NULL: the default stream).  cfg must be 2D plain FP64.
  * Work arrays live in one fixed device array of FST_NOALLOC_SCRATCH_BYTES
- * inside the library (held by every GPU that loads it until exit); grids of
- * more than FST_NOALLOC_MAX_CELLS cells including ghosts (ngi*ngj) are
- * rejected with FST_ERR_SIZE.  Nothing is allocated or freed.
+ * inside the library (held by every GPU that loads it until exit).  A call
+ * needs cells * (6 + 2 nv + 8 visc + 8 ceq) + 2 doubles of it (cells =
+ * ngi*ngj including ghosts, nv = 3 + ns); the array holds that for every
+ * mixture up to FST_MAX_SPECIES, so the limit a caller meets is
+ * FST_NOALLOC_MAX_CELLS cells: larger grids return FST_ERR_SIZE.  Nothing is
+ * allocated or freed.  Other configs (3D, mixed or hybrid mode, generalized
+ * grids) return FST_ERR_UNSUPPORTED; null pointers FST_ERR_INVALID; a CUDA
+ * error already pending from the caller's earlier work FST_ERR_CUDA, without
+ * clearing it.  Devices with an index of 64 or more are not supported.
  * The first call on each device looks up that device's copy of the array
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU (different

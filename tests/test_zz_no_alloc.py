@@ -70,6 +70,44 @@ def test_noalloc_matches_context_rhs_twice():
         assert same(R, R_ref), seed
 
 
+def test_noalloc_rejects_other_configs_and_null_pointers():
+    """Host-side checks only: every case returns before any launch."""
+    import torch
+    fn = _entry()
+    buf = torch.zeros(8, dtype=torch.float64, device="cuda")
+    p = C.c_void_p(buf.data_ptr())
+    for kw in (dict(mode=abi.MODE_MIXED), dict(mode=abi.MODE_HYBRID),
+               dict(grid_type=abi.GRID_GENERALIZED, dx=(1.0, 1.0, 1.0))):
+        cfg = abi.make_config(2, (12, 10), species=[dict(gamma=1.4, M=1.0)], R=1.0, **kw)
+        n = int(np.prod(abi.dims(cfg)))
+        assert fn(C.byref(cfg), p, p, n, None) == abi.FST_ERR_UNSUPPORTED, kw
+    cfg = abi.make_config(2, (12, 10), species=[dict(gamma=1.4, M=1.0)], R=1.0)
+    n = int(np.prod(abi.dims(cfg)))
+    assert fn(C.byref(cfg), None, p, n, None) == abi.FST_ERR_INVALID
+    assert fn(C.byref(cfg), p, None, n, None) == abi.FST_ERR_INVALID
+    assert fn(None, p, p, n, None) == abi.FST_ERR_INVALID
+    assert fn(C.byref(cfg), p, p, n + 1, None) == abi.FST_ERR_SIZE
+
+
+def test_noalloc_largest_mixture_at_the_cell_limit():
+    """The most demanding 2D config that the cell limit admits (16 species,
+    viscous, C-equation) fits the fixed array and matches the context RHS."""
+    import torch
+    fn = _entry()
+    sp = [dict(gamma=1.3 + 0.02 * s, M=1.0 + 0.1 * s, mu=2.928e-5) for s in range(16)]
+    cfg = abi.make_config(2, (122, 122), dt=1e-4, species=sp, R=1.0, visc=True, ceq=True)
+    n = int(np.prod(abi.dims(cfg)))
+    assert n // (abi.nv_of(cfg) + 5) == 128 * 128  # exactly FST_NOALLOC_MAX_CELLS cells
+    U, R_ref = _with_ghosts(cfg, 13)
+    d_U = torch.from_numpy(U.ravel(order="F")).cuda()
+    d_R = torch.full((n,), float("nan"), dtype=torch.float64, device="cuda")
+    rc = fn(C.byref(cfg), C.c_void_p(d_U.data_ptr()), C.c_void_p(d_R.data_ptr()), n,
+            C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == abi.FST_OK
+    torch.cuda.synchronize()
+    assert same(d_R.cpu().numpy().reshape(abi.dims(cfg), order="F"), R_ref)
+
+
 def test_noalloc_rejects_oversize_and_3d():
     import torch
     fn = _entry()
