@@ -285,32 +285,57 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
                                   "profiles/flux3d_plain_64cubed.md); the GB/s figures show how "
                                   "far below the HBM roof an FP64-bound kernel sits")
 
-    # end to end through the C ABI with host buffers: upload, step, download
+    # end to end through the C ABI with host buffers: upload, step, download.
+    # One untimed round trip first; then every step is bracketed by events
+    # on the library's stream around the upload, the step and the download,
+    # so the record shows the host-link rates that bound this figure.
     n_state = int(np.prod(abi.dims(cfg)))
     host = torch.empty(n_state, dtype=torch.float64, pin_memory=True)
     host.numpy()[:] = np.asfortranarray(U0).ravel(order="F")
     L = lib()
     ptr = C.cast(C.c_void_p(host.data_ptr()), C.POINTER(C.c_double))
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    e0.record(stream)
-    for _ in range(e2e_steps):
+
+    def round_trip(ev=None):
+        if ev:
+            ev[0].record(stream)
         assert L.fst_set_state(s._ctx, ptr, n_state) == 0
+        if ev:
+            ev[1].record(stream)
         assert L.fst_rk_step(s._ctx, 1) == 0
+        if ev:
+            ev[2].record(stream)
         assert L.fst_get_state(s._ctx, ptr, n_state) == 0
-    e1.record(stream)
+        if ev:
+            ev[3].record(stream)
+
+    round_trip()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
+    t0 = time.perf_counter()
+    for ev in evs:
+        round_trip(ev)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    e2e_ms = e0.elapsed_time(e1)
+    e2e_ms = evs[0][0].elapsed_time(evs[-1][3])
+    h2d = [e[0].elapsed_time(e[1]) for e in evs]
+    stp = [e[1].elapsed_time(e[2]) for e in evs]
+    d2h = [e[2].elapsed_time(e[3]) for e in evs]
     e2e_val = cells * e2e_steps / (max(e2e_ms / 1e3, wall)) / 1e6
+    nbytes = n_state * 8
+    e2e_detail = {"timed_steps": e2e_steps, "untimed_round_trips": 1,
+                  "h2d_ms_median": statistics.median(h2d),
+                  "h2d_gbs": nbytes / (statistics.median(h2d) / 1e3) / 1e9,
+                  "d2h_ms_median": statistics.median(d2h),
+                  "d2h_gbs": nbytes / (statistics.median(d2h) / 1e3) / 1e9,
+                  "step_ms_median": statistics.median(stp),
+                  "wall_s": wall, "host_buffer": "pinned (cudaHostAlloc via torch)"}
     s.close()
     return U_final, {
         "value": value, "ms_per_step": ms / steps, "gpu_launches": launches, "hybrid": hybrid_info,
         "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
         "roofline": roof, "clocks": clk.summary(), "finite": finite,
         "e2e": {"value": e2e_val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": n_state * 8,
-                "d2h_bytes_per_step": n_state * 8, "steps": e2e_steps},
+                "d2h_bytes_per_step": n_state * 8, "steps": e2e_steps, **e2e_detail},
     }
 
 
@@ -568,26 +593,42 @@ def accuracy_report(cfg, U0, finals, nsteps):
     return out
 
 
-def cpu_sample(n_sample=128, steps=1):
-    """The CPU oracle (restatement of the reference's FP64 path) on a bounded
-    sample of the same workload, all host threads."""
-    from fiesta_gb300 import abi
-    from fiesta_gb300.solver import initial_conditions
-    from oracle.oracle import Oracle
+def cpu_sample(n_sample=128, steps=3, kind=None):
+    """The reference's FP64 step on the host cores, on a bounded sample of
+    the same workload: its own sources (src/cart3d.cpp, src/rk.cpp and the
+    kernel headers, built by oracle/ref_build.sh into oracle/_ref) where that
+    library exists (kind "reference"), else the oracle restatement (kind
+    "port"); OpenMP on every host core.  The seeded initial state comes from
+    the numpy restatement of the generator (oracle/ics.py), so this leg loads
+    no product library.  Returns the median per-step rate."""
+    from oracle.ics import mixing_3d
+    from oracle.oracle import Oracle, Reference
+    if kind is None:
+        kind = "reference" if Reference.available() else "port"
     cores = os.cpu_count() or 1
-    Oracle.set_threads(cores)
     cfg = make_cfg(n_sample, 0, 1.0)
-    U0 = initial_conditions(cfg, abi.IC_MIXING_3D, SEED, **IC_KW)
+    U0 = mixing_3d(cfg, SEED, **IC_KW)
     cfg.dt = 0.5 * cfg.dx / max_wave_speed(cfg, U0)
-    o = Oracle(cfg)
+    if kind == "reference":
+        o = Reference(cfg)
+    else:
+        Oracle.set_threads(cores)
+        o = Oracle(cfg)
     o.set_state(U0)
-    t0 = time.perf_counter()
-    o.rk_step(steps)
-    dt = time.perf_counter() - t0
-    val = n_sample ** 3 * steps / dt / 1e6
-    return {"value": val, "unit": "Mcell-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} step(s) of the same case at {n_sample}^3 "
-                      f"(CPU oracle, OpenMP, {cores} threads, {dt:.1f} s)"}
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.rk_step(1)
+        times.append(time.perf_counter() - t0)
+    del o
+    per = statistics.median(times)
+    what = ("the reference's own sources (src/cart3d.cpp, src/rk.cpp, kernel headers) "
+            "built by oracle/ref_build.sh" if kind == "reference"
+            else "the CPU oracle restatement of the reference's FP64 path")
+    return {"value": n_sample ** 3 / per / 1e6, "unit": "Mcell-steps/s", "cores": cores,
+            "kind": kind,
+            "sample": f"median of {steps} step(s) of the same case at {n_sample}^3, {what}, "
+                      f"OpenMP on {cores} threads ({per:.2f} s per step)"}
 
 
 def replica_value(ms, n, world, device):
@@ -609,9 +650,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--modes", default="plain,mixed,hybrid")
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--e2e-steps", type=int, default=3)
-    # the CPU legs run one step of the full case (seconds on a 16-core host)
-    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    # the CPU legs: a bounded sample of the same case for the baseline beside
+    # the GPU line, the full case for the reference arm (the reference's own
+    # build runs ~6x slower than the oracle restatement)
+    ap.add_argument("--cpu-sample", type=int, default=128)
+    ap.add_argument("--ref-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-gen", action="store_true")
@@ -622,26 +666,27 @@ def main():
     a.warmup = max(a.warmup, 3)
 
     if a.impl == "reference":
-        # The reference has no GPU path of its own here (Kokkos is not
-        # installable); its algorithm is timed on the host cores.
+        # The reference has no GPU path here (its Kokkos CUDA build is not
+        # available); its own FP64 CPU build is timed on the host cores,
+        # with the oracle restatement beside it as a second figure.
         if rank != 0:
             return
         t0 = time.perf_counter()
-        runs = [cpu_sample(a.cpu_sample, 1) for _ in range(max(1, min(a.steps, 3)))]
-        val = statistics.median(r["value"] for r in runs)
-        cb = dict(runs[0])
-        cb["value"] = val
-        cb["sample"] += f"; median of {len(runs)} runs"
+        cb = cpu_sample(a.ref_sample, max(1, min(a.steps, 2)))
+        val = cb["value"]
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "Mcell-steps/s",
                 "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-                "ms_per_step": (a.cpu_sample ** 3) / (val * 1e6) * 1e3,
+                "ms_per_step": (a.size ** 3) / (val * 1e6) * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": workload(a.size), "grid": [a.size] * 3,
-                                                "species": 5, "sample_grid": [a.cpu_sample] * 3},
+                "data": "synthetic (seeded generator: 8 Gaussian pressure kernels, 5 species)",
+                "config": {"workload": workload(a.size), "grid": [a.size] * 3, "species": 5,
+                           "nvt": 14, "mode": "plain", "sample_grid": [a.ref_sample] * 3},
                 "cpu_baseline": cb,
                 "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0},
-                "wall_s": time.perf_counter() - t0}
+                        "d2h_bytes_per_step": 0}}
+        if cb["kind"] == "reference":
+            line["restatement"] = cpu_sample(a.ref_sample, max(1, min(a.steps, 2)), kind="port")
+        line["wall_s"] = time.perf_counter() - t0
         print(json.dumps(line))
         return
 
@@ -702,7 +747,7 @@ def main():
         if not a.no_cpu:
             gen3d["cpu_baseline"] = cpu_sample_gen3d(min(n, a.cpu_sample))
     aux = None if a.no_aux else run_aux(n, U0, dt, peak, peak_kind, cpu=not a.no_cpu)
-    cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 1)
+    cpu = None if a.no_cpu else cpu_sample(a.cpu_sample, 2)
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,

@@ -35,6 +35,29 @@ def build(force=False):
     return ORACLE_SO
 
 
+ORACLE_FMA_SO = os.path.join(HERE, "liboracle_fma.so")
+
+
+def build_fma(force=False):
+    """The same restatement compiled with multiply-add contraction on
+    (-ffp-contract=fast, FMA instructions): the rounding an FP64 build with
+    fused multiply-adds gives, as the reference's CUDA build gets from nvcc
+    by default.  Tests use the spread between the two FP64 builds as the
+    floor of what any non-bitwise implementation can hold."""
+    import platform
+    src = os.path.join(HERE, "fst_oracle.cpp")
+    if (not force and os.path.exists(ORACLE_FMA_SO)
+            and os.path.getmtime(ORACLE_FMA_SO) >= os.path.getmtime(src)):
+        return ORACLE_FMA_SO
+    cxx = os.environ.get("CXX", "g++")
+    arch = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
+    cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=fast", *arch, "-fopenmp", "-fPIC",
+           "-shared", src, "-o", ORACLE_FMA_SO + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(ORACLE_FMA_SO + ".tmp", ORACLE_FMA_SO)
+    return ORACLE_FMA_SO
+
+
 def build_reference():
     """Compile the reference sources into oracle/_ref (no-op without them)."""
     subprocess.run(["bash", os.path.join(HERE, "ref_build.sh")], check=True)
@@ -156,6 +179,21 @@ class Oracle(_Checker):
         a, b = C.c_double(), C.c_double()
         self._call("last_max", C.byref(a), C.byref(b))
         return a.value, b.value
+
+
+class OracleFMA(_Checker):
+    """The oracle built with fused multiply-adds (see build_fma)."""
+    prefix = "orc_"
+
+    @classmethod
+    def _load(cls):
+        if OracleFMA._lib is None:
+            build_fma()
+            lib = C.CDLL(ORACLE_FMA_SO)
+            lib.orc_set_threads.argtypes = [C.c_int]
+            lib.orc_set_threads(os.cpu_count() or 1)
+            OracleFMA._lib = lib
+        return OracleFMA._lib
 
 
 class Reference(_Checker):

@@ -6,7 +6,12 @@
 # the golden vectors in tests/golden/.  It is never shipped or committed.
 #
 # The reference tree is read where it lies (FST_REFERENCE, default
-# /root/reference); nothing is copied out of it.  Reference files compiled:
+# /root/reference).  A machine without it (the GPU host) builds the same
+# library from the bundle this recipe leaves in oracle/_ref/ where the tree
+# is present: the reference files these units include, and the sample decks,
+# copied into oracle/_ref/src and oracle/_ref/samples.  oracle/_ref/ is
+# git-ignored: the bundle travels with the working tree and is never
+# committed.  Reference files compiled:
 #   src/cart3d.cpp src/cart2d.cpp src/rk.cpp src/rkfunction.cpp  (-DHAVE_MPI:
 #       the single-rank MPI path, where fsMax returns an initialised maximum)
 #   src/bc.cpp  (no HAVE_MPI: periodic ghosts by bc_xPer/yPer/zPer)
@@ -20,16 +25,39 @@
 # diagnostics, metric).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${FST_REFERENCE:-/root/reference}"
 OUT="$HERE/_ref"
+REF="${FST_REFERENCE:-/root/reference}"
+STAGE=1
 if [ ! -d "$REF/src" ]; then
-  echo "ref_build: reference sources not found at $REF/src; skipping" >&2
-  exit 0
+  if [ -d "$OUT/src" ]; then
+    REF="$OUT"  # the bundle left where the reference tree was present
+    STAGE=0
+  else
+    echo "ref_build: reference sources not found at $REF/src and no bundle in $OUT; skipping" >&2
+    exit 0
+  fi
 fi
 mkdir -p "$OUT"
 CXX="${CXX:-g++}"
 FLAGS=(-std=c++17 -O2 -ffp-contract=off -fPIC -fopenmp -w
        -I "$HERE/refshim" -I "$REF/src" -include "$HERE/refshim/prelude.hpp")
+UNITS=(cart3d cart2d rk rkfunction bc gen2d gen3d)
+if [ "$STAGE" = 1 ]; then
+  mkdir -p "$OUT/src" "$OUT/samples"
+  deps=$(for u in "${UNITS[@]}"; do
+           "$CXX" "${FLAGS[@]}" -DHAVE_MPI -MM "$REF/src/$u.cpp"
+         done; "$CXX" "${FLAGS[@]}" -DHAVE_MPI -MM "$HERE/refshim/ref_harness.cpp" \
+                 "$HERE/refshim/ref_gen.cpp")
+  for f in $(echo "$deps" | tr ' \\' '\n\n' | grep "^$REF/src/" | sort -u); do
+    cp "$f" "$OUT/src/"
+  done
+  for d in "$REF"/samples/*/; do
+    if [ -f "$d/fiesta.lua" ]; then
+      mkdir -p "$OUT/samples/$(basename "$d")"
+      cp "$d/fiesta.lua" "$OUT/samples/$(basename "$d")/"
+    fi
+  done
+fi
 pids=()
 "$CXX" "${FLAGS[@]}" -DHAVE_MPI -c "$REF/src/cart3d.cpp" -o "$OUT/cart3d.o" & pids+=($!)
 "$CXX" "${FLAGS[@]}" -DHAVE_MPI -c "$REF/src/cart2d.cpp" -o "$OUT/cart2d.o" & pids+=($!)

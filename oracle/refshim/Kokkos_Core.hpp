@@ -179,20 +179,36 @@ inline void parallel_for(const std::string&, const P& p, const F& f) {
 }
 
 // Max reduction; the start value is Kokkos' reduction_identity<T>::max(),
-// i.e. the lowest finite T.
+// i.e. the lowest finite T.  Threads reduce static chunks of the outer
+// index and join with Kokkos' Max join (`if (src > dst) dst = src`, which
+// never takes a NaN), so the result is the serial maximum.
 template <class F, class T>
 inline void parallel_reduce(const MDRangePolicy<Rank<2>>& p, const F& f, Max<T> m) {
   T g = std::numeric_limits<T>::lowest();
-  for (long long i = p.b[0]; i < p.e[0]; ++i)
-    for (long long j = p.b[1]; j < p.e[1]; ++j) f((int)i, (int)j, g);
+#pragma omp parallel
+  {
+    T l = std::numeric_limits<T>::lowest();
+#pragma omp for schedule(static)
+    for (long long i = p.b[0]; i < p.e[0]; ++i)
+      for (long long j = p.b[1]; j < p.e[1]; ++j) f((int)i, (int)j, l);
+#pragma omp critical(fst_shim_max)
+    if (l > g) g = l;
+  }
   m.ref = g;
 }
 template <class F, class T>
 inline void parallel_reduce(const MDRangePolicy<Rank<3>>& p, const F& f, Max<T> m) {
   T g = std::numeric_limits<T>::lowest();
-  for (long long i = p.b[0]; i < p.e[0]; ++i)
-    for (long long j = p.b[1]; j < p.e[1]; ++j)
-      for (long long k = p.b[2]; k < p.e[2]; ++k) f((int)i, (int)j, (int)k, g);
+#pragma omp parallel
+  {
+    T l = std::numeric_limits<T>::lowest();
+#pragma omp for schedule(static)
+    for (long long i = p.b[0]; i < p.e[0]; ++i)
+      for (long long j = p.b[1]; j < p.e[1]; ++j)
+        for (long long k = p.b[2]; k < p.e[2]; ++k) f((int)i, (int)j, (int)k, l);
+#pragma omp critical(fst_shim_max)
+    if (l > g) g = l;
+  }
   m.ref = g;
 }
 

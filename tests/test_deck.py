@@ -148,10 +148,13 @@ r = math.max(3, 9, 4) + math.floor(2.7) + math.sqrt(16)
     assert G["q"] == 720 and G["r"] == 9 + 2 + 4.0
 
 
-SAMPLES = os.path.join(os.environ.get("FST_REFERENCE", "/root/reference"), "samples")
+# the reference's sample decks, staged by oracle/ref_build.sh next to the
+# reference checker it builds
+SAMPLES = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle",
+                       "_ref", "samples")
 
 
-@pytest.mark.skipif(not os.path.isdir(SAMPLES), reason="reference samples not present")
+@pytest.mark.skipif(not os.path.isdir(SAMPLES), reason="reference sample decks not staged")
 def test_reference_sample_decks():
     """The decks written for the current reader load; the legacy flat-global
     decks fail on their first required key, as with the reference."""

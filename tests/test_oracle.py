@@ -177,3 +177,36 @@ def test_oracle_matches_reference_degenerate_periodic(n):
     o.rk_step(2)
     r.rk_step(2)
     assert same(o.get_state(), r.get_state())
+
+
+@pytest.mark.parametrize("n", [(24, 20, 16), (33, 17, 19)])
+def test_numpy_mixing_ic_equals_compiled_generator(n):
+    """The numpy restatement of the mixing generator (oracle/ics.py, used by
+    the benchmark's reference arm, which loads no product library) gives the
+    compiled generator's bits."""
+    from fiesta_gb300.solver import initial_conditions
+    from oracle.ics import mixing_3d
+    sp = [dict(gamma=g, M=m / 1000.0, mu=1e-5) for g, m in
+          zip([1.4, 1.67, 1.3, 1.32, 1.4], [28.96, 4.0, 44.0, 16.0, 2.0])]
+    cfg = abi.make_config(3, n, species=sp, visc=True, ceq=True)
+    kw = dict(p_ambient=1e5, T_ambient=300.0, nkernels=8)
+    A = initial_conditions(cfg, abi.IC_MIXING_3D, 20261206, **kw)
+    B = mixing_3d(cfg, 20261206, **kw)
+    assert A.shape == B.shape and np.array_equal(A.view(np.uint64), B.view(np.uint64))
+
+
+def test_fma_build_of_the_oracle_differs_only_by_rounding():
+    """The FMA-contracted oracle build (the rounding spread tests use as the
+    floor for the C-equation fields) agrees with the strict build to
+    rounding on a smooth case."""
+    from fiesta_gb300.solver import initial_conditions
+    from oracle.oracle import OracleFMA
+    cfg = abi.make_config(3, (12, 10, 8), dt=1e-4, species=[dict(gamma=1.4, M=1.0, mu=1e-3)],
+                          R=1.0, visc=True, ceq=True)
+    U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 2)
+    a, b = Oracle(cfg), OracleFMA(cfg)
+    for x in (a, b):
+        x.set_state(U0)
+        x.rk_step(2)
+    Ua, Ub = a.get_state(), b.get_state()
+    assert np.allclose(Ua, Ub, rtol=1e-12, atol=0)
