@@ -202,6 +202,8 @@ void setup_phys(const fst_config& cf, const Geo& g, Phys& P) {
     P.rm_s[s] = P.cp_s[s] - P.cv_s[s];
     P.cv_f[s] = (float)P.cv_s[s];
     P.rm_f[s] = (float)(P.cp_s[s] - P.cv_s[s]);
+    P.cv_lf[s] = (float)(P.cv_s[s] - (double)P.cv_f[s]);
+    P.rm_lf[s] = (float)(P.rm_s[s] - (double)P.rm_f[s]);
     P.mu_f[s] = (float)P.mu_s[s];
     P.cv2_f[s] = (float)P.cv2_s[s];
     P.cp2_f[s] = (float)P.cp2_s[s];
@@ -521,6 +523,7 @@ int fst_synchronize(fst_ctx* c) {
 int fst_set_state(fst_ctx* c, const double* U, size_t n) {
   if (!c || !U) return FST_ERR_INVALID;
   if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  c->bm.fused_for = nullptr;  // the primitives no longer describe the state
   cudaError_t e = cudaMemcpyAsync(c->Ua, U, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "set_state");
@@ -539,6 +542,7 @@ int fst_get_state(fst_ctx* c, double* U, size_t n) {
 int fst_set_state_device(fst_ctx* c, const double* dU, size_t n) {
   if (!c || !dU) return FST_ERR_INVALID;
   if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  c->bm.fused_for = nullptr;
   cudaError_t e = cudaMemcpyAsync(c->Ua, dU, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "set_state_device");
   return FST_OK;
@@ -746,6 +750,7 @@ int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
   if (c->gen && c->g.ndim == 3)
     return fail(c, FST_ERR_UNSUPPORTED, "the generalized 3D module has no noise filter");
   if (np->nt < 0) return fail(c, FST_ERR_INVALID, "noise nt must be >= 0");
+  c->bm.fused_for = nullptr;  // the filter changes the state's interior
   const Geo& g = c->g;
   if (!c->dnoise) {  // zero-initialised like the module's FS3D_I / FS2D_I
     const size_t ints = (size_t)fst_noise_ints(g);
@@ -810,6 +815,7 @@ int fst_hybrid_features(fst_ctx* c, float* d_features, unsigned char* d_labels, 
     int rc = bcs(c, c->Ua);
     if (rc) return rc;
   }
+  c->bm.fused_for = nullptr;
   c->stats.kernel_launches += fst_mixed_prims(c->g, c->P, c->cf, c->bm, c->Ua, c->stream);
   const MixedView M{c->bm.Q,   c->bm.rho32, c->bm.vel32, c->bm.p64,   c->bm.mu32, c->bm.nrg,
                     c->bm.C,   c->bm.T32,   c->bm.rho64, c->bm.p32};

@@ -55,6 +55,8 @@ struct Phys {
   // FP32 copies for the mixed path: cv_s, R_s = cp_s - cv_s, mu_s, and the
   // stride-2 table constants
   float cv_f[FST_MAX_SPECIES], rm_f[FST_MAX_SPECIES], mu_f[FST_MAX_SPECIES];
+  // low parts of cv_s and R_s as FP32 pairs (cv_f + cv_lf, rm_f + rm_lf)
+  float cv_lf[FST_MAX_SPECIES], rm_lf[FST_MAX_SPECIES];
   float cv2_f[FST_MAX_SPECIES], cp2_f[FST_MAX_SPECIES];
   // FP32 copies of the grid constants (mixed path)
   float rd_f[3];    // 1/dx, 1/dy, 1/dz

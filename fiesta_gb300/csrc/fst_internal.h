@@ -105,6 +105,14 @@ int fst_plain2d_secondary(const Geo& g, const Phys& P, const Plain2DBufs& b, con
 
 // fst_mixed.cu (FST_MODE_MIXED / FST_MODE_HYBRID)
 struct Mixed3DMaps;  // TMA tensor maps of the 3D primitive arrays (fst_mixed3d.cu)
+// The second set of 3D primitive arrays, the tensor maps over them and its
+// reduction words (see MixedBufs::fused)
+struct PrimSet {
+  float *Q, *rho32, *vel32, *mu32, *nrg, *C, *p32, *plo;
+  double* rho64;
+  Mixed3DMaps* maps3d;
+  unsigned long long* red;
+};
 struct MixedBufs {
   // Geometry of the primitive arrays.  2D: the state's.  3D: rows padded to
   // a multiple of 4 floats so that every row, plane and field starts on a
@@ -116,6 +124,9 @@ struct MixedBufs {
   double* p64;    // FP64 pressure (2D)
   float* p32;     // pressure as an FP32 pair: hi [cells], lo [cells] (3D)
   double* rho64;  // FP64 density (buoyancy source)
+  // 3D C-equation runs: low parts of the FP32 pairs of rho, nrg, u, v, w
+  // ([5][cells], see Prim3Out) for the shock/contact switches
+  float* plo;
   // FP64 secondary outputs (fst_secondary)
   double *rho, *pr, *vel, *T;
   unsigned long long* red;
@@ -141,7 +152,17 @@ struct MixedBufs {
   // and its FP32 pairs hi [9] + lo [9] in the primitives' layout
   double* met64;
   float* metf;
+  // Fused 3D stages (cartesian, up to 5 species): the last kernel of a stage
+  // writes the primitives of U_new's interior into `alt`, which becomes the
+  // current set for the next stage; its ghost cells are filled after the
+  // boundary conditions.  fused_for: the state whose interior primitives the
+  // current set holds (null when none does, e.g. after the state was set).
+  bool fused;
+  PrimSet alt;
+  const double* fused_for;
 };
+// exchange the current primitive set with b.alt
+void fst_mixed_swap(MixedBufs& b);
 struct MixedView {
   const float* Q;    // [nv][cells] conserved variables, Q[ndim] = E + p
   const float* rho;  // [cells]
@@ -153,6 +174,7 @@ struct MixedView {
   const float* T;    // [cells] (2D viscous heat flux)
   const double* rho64;  // [cells] FP64 density (buoyancy)
   const float* pp;      // [2][cells] pressure hi + lo (3D)
+  const float* lo;      // [5][cells] low parts of rho, nrg, u, v, w (3D C-equation)
 };
 using fst_alloc_fn = std::function<int(void**, size_t)>;
 size_t fst_mixed_work_doubles_per_cell(const fst_config& cf, const Geo& g);
@@ -201,6 +223,7 @@ int fst_noise_launch(const Geo& g, const fst_config& cf, double* U, int* noise,
 Geo fst_prim_geo(const Geo& g);
 int fst_mixed3d_prepare(const Geo& g, MixedBufs& b, std::string* why);
 void fst_mixed3d_release(MixedBufs& b);
+// fused: the stage also writes the primitives of U_new's interior into b.alt
 int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
                     const unsigned char* smooth, const double* Uold, double* Unew, double coef,
-                    double* Rout, cudaStream_t st, Prof* prof, bool hybrid);
+                    double* Rout, cudaStream_t st, Prof* prof, bool hybrid, bool fused);

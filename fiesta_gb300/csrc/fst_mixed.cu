@@ -24,6 +24,9 @@
 // src/ceq3d.hpp, src/presgrad.hpp, src/buoyancy.hpp); only the arithmetic
 // precision differs.  The error against the FP64 oracle is measured by
 // tests/test_gpu_mixed.py.
+#include <cstdlib>
+#include <utility>
+
 #include "fst_mixed_dev.cuh"
 
 namespace {
@@ -54,6 +57,64 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const doub
       atomicMax(&red[1], fst_key((double)lC));
     }
   }
+}
+
+// 3D: the FP64-free equation of state of mprim3_cell, same grid as k_mprim
+template <int NS>
+__global__ void __launch_bounds__(256) k_mprim3(Geo g, Geo gq, Phys P,
+                                                const double* __restrict__ U, Prim3Out O,
+                                                unsigned long long* __restrict__ red) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  const int j = t / g.ngi, i = t - j * g.ngi;
+  float lS = -3.0e38f, lC = -3.0e38f;
+  if (j < g.ngj) mprim3_cell<NS>(g, gq, P, U, O, red != nullptr, i, j, blockIdx.z, lS, lC);
+  if (red) {
+    lS = warp_maxf(lS);
+    lC = warp_maxf(lC);
+    if ((threadIdx.x & 31) == 0 && lS > -1e38f) {
+      atomicMax(&red[0], fst_key((double)lS));
+      atomicMax(&red[1], fst_key((double)lC));
+    }
+  }
+}
+
+// The ghost cells of the 3D primitive pass: the 2*ng ghost planes in k, the
+// ghost rows in j of the interior planes, the ghost columns in i of the
+// interior rows, one thread per cell.  Fused stages compute the interior in
+// the previous stage's last kernel and only these after the boundary fill.
+template <int NS>
+__global__ void __launch_bounds__(256) k_mprim3_shell(Geo g, Geo gq, Phys P,
+                                                      const double* __restrict__ U, Prim3Out O) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  const int ng = g.ng, nk = g.ngk - 2 * ng, nj = g.ngj - 2 * ng;
+  const long long pl = (long long)g.ngi * g.ngj;
+  const long long nA = 2LL * ng * pl;                   // ghost planes
+  const long long nB = (long long)nk * 2 * ng * g.ngi;  // ghost rows of interior planes
+  const long long nC = (long long)nk * nj * 2 * ng;     // ghost columns of interior rows
+  int i, j, k;
+  if (t < nA) {
+    const long long p = t / pl, r = t - p * pl;
+    k = p < ng ? (int)p : g.ngk - 2 * ng + (int)p;
+    j = (int)(r / g.ngi);
+    i = (int)(r - (long long)j * g.ngi);
+  } else if (t < nA + nB) {
+    const long long u = t - nA, row = u / g.ngi;
+    i = (int)(u - row * g.ngi);
+    const int kk = (int)(row / (2 * ng)), jj = (int)(row - (long long)kk * 2 * ng);
+    k = ng + kk;
+    j = jj < ng ? jj : g.ngj - 2 * ng + jj;
+  } else if (t < nA + nB + nC) {
+    const long long u = t - nA - nB, row = u / (2 * ng);
+    const int ii = (int)(u - row * 2 * ng);
+    const int kk = (int)(row / nj), jj = (int)(row - (long long)kk * nj);
+    k = ng + kk;
+    j = ng + jj;
+    i = ii < ng ? ii : g.ngi - 2 * ng + ii;
+  } else {
+    return;
+  }
+  float lS = 0.f, lC = 0.f;
+  mprim3_cell<NS>(g, gq, P, U, O, false, i, j, k, lS, lC);
 }
 
 template <int NV, bool HYB>
@@ -93,6 +154,42 @@ void launch_mprim(const Geo& g, const Geo& gq, const Phys& P, const double* U, f
                   float* nrg, float* Cc, float* T, unsigned long long* red, cudaStream_t st) {
   const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
   k_mprim<NDIM><<<qg, qb, 0, st>>>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red);
+}
+
+Prim3Out prim3_out(const Phys& P, const MixedBufs& b, bool all_outputs) {
+  const bool visc = all_outputs || P.visc, ceq = all_outputs || P.ceq;
+  return Prim3Out{b.Q, b.rho32, b.vel32, b.p32, visc ? b.mu32 : nullptr, ceq ? b.nrg : nullptr,
+                  ceq ? b.C : nullptr, ceq ? b.plo : nullptr, b.rho64};
+}
+
+// the 3D primitive pass over all cells (shell = false) or the ghost cells only
+void launch_mprim3(const Geo& g, const Phys& P, const MixedBufs& b, const double* U,
+                   bool all_outputs, unsigned long long* red, cudaStream_t st,
+                   bool shell = false) {
+  const Prim3Out O = prim3_out(P, b, all_outputs);
+  if (shell) {
+    const long long nk = g.ngk - 2 * g.ng, nj = g.ngj - 2 * g.ng;
+    const long long n = 2LL * g.ng * g.ngi * g.ngj + nk * 2 * g.ng * g.ngi + nk * nj * 2 * g.ng;
+    const unsigned nb = cdiv(n, 256);
+    switch (g.ns) {
+      case 1: k_mprim3_shell<1><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
+      case 2: k_mprim3_shell<2><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
+      case 3: k_mprim3_shell<3><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
+      case 4: k_mprim3_shell<4><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
+      case 5: k_mprim3_shell<5><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
+      default: k_mprim3_shell<0><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
+    }
+    return;
+  }
+  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
+  switch (g.ns) {
+    case 1: k_mprim3<1><<<qg, qb, 0, st>>>(g, b.gq, P, U, O, red); break;
+    case 2: k_mprim3<2><<<qg, qb, 0, st>>>(g, b.gq, P, U, O, red); break;
+    case 3: k_mprim3<3><<<qg, qb, 0, st>>>(g, b.gq, P, U, O, red); break;
+    case 4: k_mprim3<4><<<qg, qb, 0, st>>>(g, b.gq, P, U, O, red); break;
+    case 5: k_mprim3<5><<<qg, qb, 0, st>>>(g, b.gq, P, U, O, red); break;
+    default: k_mprim3<0><<<qg, qb, 0, st>>>(g, b.gq, P, U, O, red); break;
+  }
 }
 
 // Launch the fused 2D RHS for a compile-time variable count.
@@ -151,6 +248,7 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   if (cf.ceq) {
     A((void**)&b.nrg, sizeof(float) * n);
     A((void**)&b.C, sizeof(float) * n * 5);
+    if (g.ndim == 3) A((void**)&b.plo, sizeof(float) * n * 5);
   }
   A((void**)&b.rho, sizeof(double) * ns);
   A((void**)&b.pr, sizeof(double) * ns);
@@ -163,13 +261,51 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
     A((void**)&b.met64, sizeof(double) * ns * 9);
     A((void**)&b.metf, sizeof(float) * n * 18);
   }
+  // fused 3D stages: cartesian grids whose species fit one species launch
+  // (FST_MIXED_UNFUSED=1 runs the separate primitive pass instead, which
+  // gives the same bits; the tests compare the two)
+  const char* unf = getenv("FST_MIXED_UNFUSED");
+  b.fused = g.ndim == 3 && cf.grid_type == FST_GRID_CARTESIAN && g.ns <= 5 &&
+            !(unf && unf[0] == '1');
+  b.fused_for = nullptr;
+  if (b.fused) {
+    PrimSet& a = b.alt;
+    A((void**)&a.Q, sizeof(float) * n * g.nv);
+    A((void**)&a.rho32, sizeof(float) * n);
+    A((void**)&a.vel32, sizeof(float) * n * 3);
+    A((void**)&a.p32, sizeof(float) * n * 2);
+    if (cf.buoyancy) A((void**)&a.rho64, sizeof(double) * n);
+    if (cf.visc) A((void**)&a.mu32, sizeof(float) * n);
+    if (cf.ceq) {
+      A((void**)&a.nrg, sizeof(float) * n);
+      A((void**)&a.C, sizeof(float) * n * 5);
+      A((void**)&a.plo, sizeof(float) * n * 5);
+    }
+    A((void**)&a.red, sizeof(unsigned long long) * 2);
+  }
   if (!rc && cf.mode == FST_MODE_HYBRID) rc = fst_hybrid_alloc(cf, g, b, alloc);
   if (!rc) rc = fst_mixed3d_prepare(g, b, why);
   return rc;
 }
 
+void fst_mixed_swap(MixedBufs& b) {
+  PrimSet& a = b.alt;
+  std::swap(b.Q, a.Q);
+  std::swap(b.rho32, a.rho32);
+  std::swap(b.vel32, a.vel32);
+  std::swap(b.mu32, a.mu32);
+  std::swap(b.nrg, a.nrg);
+  std::swap(b.C, a.C);
+  std::swap(b.p32, a.p32);
+  std::swap(b.plo, a.plo);
+  std::swap(b.rho64, a.rho64);
+  std::swap(b.maps3d, a.maps3d);
+  std::swap(b.red, a.red);
+}
+
 cudaError_t fst_mixed_canary(const Geo& g, const MixedBufs& b, cudaStream_t st) {
   const size_t n = (size_t)b.gq.sv;
+  const PrimSet& a = b.alt;
   const struct {
     void* p;
     size_t bytes;
@@ -177,7 +313,12 @@ cudaError_t fst_mixed_canary(const Geo& g, const MixedBufs& b, cudaStream_t st) 
            {b.vel32, sizeof(float) * n * g.ndim}, {b.mu32, sizeof(float) * n},
            {b.T32, sizeof(float) * n}, {b.nrg, sizeof(float) * n},
            {b.C, sizeof(float) * n * 5}, {b.p32, sizeof(float) * n * 2},
-           {b.p64, sizeof(double) * n}, {b.metf, sizeof(float) * n * 18}};
+           {b.p64, sizeof(double) * n}, {b.metf, sizeof(float) * n * 18},
+           {b.plo, sizeof(float) * n * 5}, {a.Q, sizeof(float) * n * g.nv},
+           {a.rho32, sizeof(float) * n}, {a.vel32, sizeof(float) * n * 3},
+           {a.mu32, sizeof(float) * n}, {a.nrg, sizeof(float) * n},
+           {a.C, sizeof(float) * n * 5}, {a.p32, sizeof(float) * n * 2},
+           {a.plo, sizeof(float) * n * 5}};
   cudaError_t e = cudaSuccess;
   for (const auto& x : f)
     if (x.p && e == cudaSuccess) e = cudaMemsetAsync(x.p, 0xFF, x.bytes, st);
@@ -188,15 +329,22 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
                     const double* Uin, const double* Uold, double* Unew, double coef, double* Rout,
                     bool ghosts, cudaStream_t st, Prof* prof) {
   int n = 0;
-  if (P.ceq) {
-    fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
-  }
-  const MixedView M{b.Q, b.rho32, b.vel32, b.p64, b.mu32, b.nrg, b.C, b.T32, b.rho64, b.p32};
-  if (g.ndim == 3) {
+  // Fused 3D stages: the previous stage left the primitives of Uin's interior
+  // (and the C-equation maxima) in the current set; only the ghost cells,
+  // just filled by the boundary conditions, remain.  Otherwise (first stage
+  // after the state was set, a bare RHS) the whole primitive pass runs.
+  const bool fuse = b.fused && !Rout && !b.metf;
+  const bool have = fuse && b.fused_for == Uin;
+  if (!fuse) b.fused_for = nullptr;
+  if (P.ceq && !have) fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
+  if (fuse) fst_fill_keys(b.alt.red, 2, FST_KEY_LOWEST, st);
+  const MixedView M{b.Q, b.rho32, b.vel32, b.p64,  b.mu32,
+                    b.nrg, b.C, b.T32, b.rho64, b.p32, b.plo};
+  if (g.ndim == 3 && have) {
+    FST_LAUNCH(prof, "mprim3d_shell", st, n, launch_mprim3(g, P, b, Uin, false, nullptr, st, true));
+  } else if (g.ndim == 3) {
     FST_LAUNCH(prof, "mprim3d", st, n,
-               launch_mprim<3>(g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32,
-                               P.visc ? b.mu32 : nullptr, P.ceq ? b.nrg : nullptr,
-                               P.ceq ? b.C : nullptr, nullptr, P.ceq ? b.red : nullptr, st));
+               launch_mprim3(g, P, b, Uin, false, P.ceq ? b.red : nullptr, st));
     if (b.metf)  // generalized grid: contravariant velocity for the face kernels
       FST_LAUNCH(prof, "gen_tvel", st, n, fst_mixedgen_tvel(g, b.gq, b.metf, b.vel32, st));
   } else {
@@ -221,7 +369,7 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     if (audit) hyb = false;
   }
   if (g.ndim == 3)
-    n += fst_mixed3d_rhs(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, prof, hyb);
+    n += fst_mixed3d_rhs(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, prof, hyb, fuse);
   else if (hyb)
     FST_LAUNCH(prof, "mrhs2d_hybrid", st, n,
                dispatch_rhs<true>(g, P, M, b.red, smooth, Uold, Unew, coef, Rout, st));
@@ -231,6 +379,10 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
   if (ghosts && !Rout)
     FST_LAUNCH(prof, "mghost", st, n,
                k_mghost<<<dim3(g.ngj, g.ngk), 64, 0, st>>>(g, Uold, Unew));
+  if (fuse) {  // the next stage reads what this one wrote into the other set
+    fst_mixed_swap(b);
+    b.fused_for = Unew;
+  }
   return n;
 }
 
@@ -258,8 +410,7 @@ int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const Mix
                     const double* U, cudaStream_t st) {
   (void)cf;
   if (g.ndim == 3)
-    launch_mprim<3>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, nullptr, b.p32, b.mu32, b.nrg,
-                    b.C, nullptr, nullptr, st);
+    launch_mprim3(g, P, b, U, true, nullptr, st);
   else
     launch_mprim<2>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, nullptr, b.nrg,
                     b.C, b.T32, nullptr, st);

@@ -1,13 +1,14 @@
 // fst_mixed3d.cu — the 3D mixed-precision (FST_MODE_MIXED) and learned-hybrid
 // (FST_MODE_HYBRID) right-hand side + RK stage for sm_103a.
 //
-// Three 2.5D stencil kernels per stage, each updating its own conserved
+// Four 2.5D stencil kernels per stage, each updating its own conserved
 // variables of U_new = U_old + coef*R in FP64 (R never goes to HBM):
 //
-//   k_mcell3d  the cell-centred terms: the FP64 pressure gradient
-//              (src/presgrad.hpp:41-74) and buoyancy (src/buoyancy.hpp) of
-//              the momenta and energy, U_new = U_old + coef*R_cell, and the
-//              five C-equation variables (updateCeq, src/ceq3d.hpp:160-230)
+//   k_mcell3d  the cell-centred terms of the momenta and energy: the
+//              FP64-accurate pressure gradient (src/presgrad.hpp:41-74) and
+//              buoyancy (src/buoyancy.hpp), U_new = U_old + coef*R_cell
+//   k_mceq3d   the five C-equation variables (calculateRhoGrad, updateCeq,
+//              src/ceq3d.hpp:95-224)
 //   k_mspec3d  species densities: WENO5 advection, their only term
 //   k_mmom3d   momenta and energy: WENO5 advection, the viscous stress
 //              (calculateStressTensor{x,y,z}3dv, src/viscosity.hpp) and the
@@ -57,6 +58,7 @@ struct Mixed3DMaps {
   CUtensorMap c5;   // C-variables 0..4
   CUtensorMap c4;   // C-variables 1..4 (C_hat, C_1..3)
   CUtensorMap p;    // pressure hi/lo pair (2 FP32 fields)
+  CUtensorMap lo4;  // pair low parts 0..3 (rho, e, u, v)
   int nsc;          // species per k_mspec3d launch
 };
 
@@ -161,18 +163,30 @@ __host__ __device__ inline MomLayout mom_layout(bool visc, bool ceq) {
   return L;
 }
 struct CellLayout {
-  int p, v, rho, nrg, c, size;  // p: pressure hi plane then lo plane
+  int p, v, size;  // p: pressure hi plane then lo plane; v: u, v
   uint32_t bytes;
 };
-__host__ __device__ inline CellLayout cell_layout(bool ceq) {
+__host__ __device__ inline CellLayout cell_layout() {
   CellLayout L;
   L.p = 0;
   L.v = al32(2 * PL);
-  L.rho = al32(L.v + 2 * PL);
+  L.size = al32(L.v + 2 * PL);
+  L.bytes = (uint32_t)(4 * PL * 4);
+  return L;
+}
+struct CeqLayout {
+  int v, rho, nrg, c, lo, size;  // lo: pair low parts of rho, e, u, v
+  uint32_t bytes;
+};
+__host__ __device__ inline CeqLayout ceq_layout() {
+  CeqLayout L;
+  L.v = 0;
+  L.rho = al32(2 * PL);
   L.nrg = al32(L.rho + PL);
   L.c = al32(L.nrg + PL);
-  L.size = ceq ? al32(L.c + 5 * PL) : L.rho;
-  L.bytes = (uint32_t)((2 + 2 + (ceq ? 7 : 0)) * PL * 4);
+  L.lo = al32(L.c + 5 * PL);
+  L.size = al32(L.lo + 4 * PL);
+  L.bytes = (uint32_t)(13 * PL * 4);
   return L;
 }
 
@@ -181,17 +195,35 @@ __device__ __forceinline__ unsigned char* aligned_smem(unsigned char* p) {
 }
 
 // ---------------------------------------------------------------------------
-// k_mcell3d: pressure gradient, buoyancy, C-equation variables
+// k_mcell3d: pressure gradient and buoyancy of the momenta and energy
+// k_mceq3d:  the five C-equation variables (updateCeq)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(TX * TY, 2)
+// Fourth-order central derivative of an FP32-pair field from its high parts
+// h and low parts l at offsets -2o .. 2o: the differences of neighbouring
+// high parts are exact for close values and carry the low parts, so the
+// result has FP32 accuracy relative to the derivative itself, not to the
+// field's values.
+__device__ __forceinline__ float d4pair(const float* h, const float* l, int o, float r12) {
+  const float d1 = (h[o] - h[-o]) + (l[o] - l[-o]);
+  const float d2 = (h[2 * o] - h[-2 * o]) + (l[2 * o] - l[-2 * o]);
+  return (8.0f * d1 - d2) * r12;
+}
+// the same along z from 5-plane windows (w[m] = plane k-2+m)
+__device__ __forceinline__ float d4pairz(const float h[5], const float l[5], float r12) {
+  const float d1 = (h[3] - h[1]) + (l[3] - l[1]);
+  const float d2 = (h[4] - h[0]) + (l[4] - l[0]);
+  return (8.0f * d1 - d2) * r12;
+}
+
+__global__ void __launch_bounds__(TX * TY, 3)
     k_mcell3d(const __grid_constant__ Mixed3DMaps maps, Geo g, Geo gq, Phys P, MixedView M,
-              const unsigned long long* __restrict__ red, const double* Uold, double* Unew,
-              double coef, double* __restrict__ Rout, unsigned int* __restrict__ err) {
+              const double* Uold, double* Unew, double coef, double* __restrict__ Rout,
+              unsigned int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smdyn[];
   unsigned char* smraw = aligned_smem(smdyn);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
-  const bool ceq = P.ceq != 0, buoy = P.buoyancy != 0;
-  const CellLayout L = cell_layout(ceq);
+  const bool buoy = P.buoyancy != 0;
+  const CellLayout L = cell_layout();
   float* tiles = reinterpret_cast<float*>(smraw + BAR_BYTES);
   const int tid = threadIdx.y * TX + threadIdx.x;
   const Place pl = place_cells(g);
@@ -202,8 +234,6 @@ __global__ void __launch_bounds__(TX * TY, 2)
   const long long cq0 = (long long)i + gq.sy * j;
   const long long c0 = (long long)i + g.sy * j;
   const long long sz = gq.sz;
-  float maxS;
-  const FaceCtx fc = make_ctx(P, red, &maxS);
   if (tid == 0) {
     prefetch_map(&maps.p);
     prefetch_map(&maps.v2);
@@ -217,56 +247,30 @@ __global__ void __launch_bounds__(TX * TY, 2)
     mbar_arrive_expect_tx(&bar[buf], L.bytes);
     tma_load_4d(tb + L.p, &maps.p, &bar[buf], pl.x0, pl.y0, k, 0);
     tma_load_4d(tb + L.v, &maps.v2, &bar[buf], pl.x0, pl.y0, k, 0);
-    if (ceq) {
-      tma_load_4d(tb + L.rho, &maps.rho, &bar[buf], pl.x0, pl.y0, k, 0);
-      tma_load_4d(tb + L.nrg, &maps.nrg, &bar[buf], pl.x0, pl.y0, k, 0);
-      tma_load_4d(tb + L.c, &maps.c5, &bar[buf], pl.x0, pl.y0, k, 0);
-    }
   };
   if (tid == 0) {
     issue(0);
     if (kc0 + 1 < kc1) issue(1);
   }
-  // own-column windows: p (hi, lo), rho, e, w at k-2 .. k+2 (+ next), C at
-  // k-1 .. k+1 (+ next)
-  const float* vz = M.vel + 2 * gq.sv;
+  // own-column window of the pressure pair at planes k-2 .. k+2 (+ next)
   const float* plo = M.pp + gq.sv;
   float ph[5], pl5[5], phn = 0.f, pln = 0.f;
-  float rw[5], ew[5], ww[5], cw[5][3], rn = 0.f, en = 0.f, wn = 0.f, cn[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) {
     const long long o = cq0 + sz * (kc0 - 3 + m);  // planes kc0-3 .. kc0+1, shifted in below
     ph[m] = cell ? M.pp[o] : 0.f;
     pl5[m] = cell ? plo[o] : 0.f;
-    ww[m] = cell ? vz[o] : 0.f;
-    rw[m] = (cell && ceq) ? M.rho[o] : 0.f;
-    ew[m] = (cell && ceq) ? M.nrg[o] : 0.f;
   }
   if (cell) {
-    const long long o = cq0 + sz * (kc0 + 2);
-    phn = M.pp[o];
-    pln = plo[o];
-    wn = vz[o];
-    if (ceq) {
-      rn = M.rho[o];
-      en = M.nrg[o];
-    }
+    phn = M.pp[cq0 + sz * (kc0 + 2)];
+    pln = plo[cq0 + sz * (kc0 + 2)];
   }
-#pragma unroll
-  for (int q = 0; q < 5; ++q) {
-#pragma unroll
-    for (int m = 0; m < 3; ++m)
-      cw[q][m] = (cell && ceq) ? M.C[cq0 + gq.sv * q + sz * (kc0 - 2 + m)] : 0.f;
-    cn[q] = (cell && ceq) ? M.C[cq0 + gq.sv * q + sz * (kc0 + 1)] : 0.f;
-  }
-  // old state of this kernel's variables: 0..3 and the C-variables
-  double uo[9], un[9];
+  // old state of the momenta and energy, one plane ahead
+  double uo[4], un[4];
   auto load_old = [&](int k, double* u) {
     const long long c = c0 + g.sz * k;
 #pragma unroll
     for (int w = 0; w < 4; ++w) u[w] = Uold[c + g.sv * w];
-#pragma unroll
-    for (int q = 0; q < 5; ++q) u[4 + q] = ceq ? Uold[c + g.sv * (P.nv + q)] : 0.0;
   };
   if (cell && !Rout) load_old(kc0, un);
 
@@ -274,63 +278,34 @@ __global__ void __launch_bounds__(TX * TY, 2)
   int k = kc0;
   for (; k < kc1; ++k) {
     const int n = k - kc0, b = n % NBUF;
-    // windows -> k-2 .. k+2 (C: k-1 .. k+1); fetch the next planes
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       ph[m] = ph[m + 1];
       pl5[m] = pl5[m + 1];
-      ww[m] = ww[m + 1];
-      rw[m] = rw[m + 1];
-      ew[m] = ew[m + 1];
     }
     ph[4] = phn;
     pl5[4] = pln;
-    ww[4] = wn;
-    rw[4] = rn;
-    ew[4] = en;
 #pragma unroll
-    for (int q = 0; q < 5; ++q) {
-      cw[q][0] = cw[q][1];
-      cw[q][1] = cw[q][2];
-      cw[q][2] = cn[q];
-    }
-#pragma unroll
-    for (int w = 0; w < 9; ++w) uo[w] = un[w];
+    for (int w = 0; w < 4; ++w) uo[w] = un[w];
     if (cell && k + 1 < kc1) {
-      const long long o = cq0 + sz * (k + 3);
-      phn = M.pp[o];
-      pln = plo[o];
-      wn = vz[o];
-      if (ceq) {
-        rn = M.rho[o];
-        en = M.nrg[o];
-#pragma unroll
-        for (int q = 0; q < 5; ++q) cn[q] = M.C[cq0 + gq.sv * q + sz * (k + 2)];
-      }
+      phn = M.pp[cq0 + sz * (k + 3)];
+      pln = plo[cq0 + sz * (k + 3)];
       if (!Rout) load_old(k + 1, un);
     }
     ok = ok && mbar_wait(&bar[b], (uint32_t)((n / NBUF) & 1), err);
     if (cell && ok) {
       const float* tb = tiles + b * L.size;
-      // 4th-order pressure gradient from the hi/lo pair: the differences of
-      // neighbouring pressures are exact in FP32 for the hi parts (close
-      // values) and carry the lo parts, so only the final combination rounds
+      // 4th-order pressure gradient (src/presgrad.hpp:44-71) from the hi/lo
+      // pair; reference quirk: the z spacing is dy
       const float* th = tb + L.p + pl.own;
       const float* tl = th + PL;
-      auto dif = [](float ha, float la, float hb, float lb) { return (ha - hb) + (la - lb); };
-      const float dpx = (8.0f * dif(th[1], tl[1], th[-1], tl[-1]) - dif(th[2], tl[2], th[-2], tl[-2])) *
-                        P.r12_f[0];
-      const float dpy = (8.0f * dif(th[HX], tl[HX], th[-HX], tl[-HX]) -
-                         dif(th[2 * HX], tl[2 * HX], th[-2 * HX], tl[-2 * HX])) *
-                        P.r12_f[1];
-      // reference quirk: the z spacing of the pressure gradient is dy
-      const float dpz = (8.0f * dif(ph[3], pl5[3], ph[1], pl5[1]) - dif(ph[4], pl5[4], ph[0], pl5[0])) *
-                        P.r12_f[1];
+      const float dpx = d4pair(th, tl, 1, P.r12_f[0]);
+      const float dpy = d4pair(th, tl, HX, P.r12_f[1]);
+      const float dpz = d4pairz(ph, pl5, P.r12_f[1]);
       double Rd[4] = {-f2d(dpx), -f2d(dpy), -f2d(dpz), 0.0};
-      const float* tu = tb + L.v + pl.own;
-      if (buoy) {
-        const long long cqk = cq0 + sz * k;
-        const double f = -P.g * (M.rho64[cqk] - P.rho_ref);
+      if (buoy) {  // computeBuoyancy3D (src/buoyancy.hpp:22-47)
+        const float* tu = tb + L.v + pl.own;
+        const double f = -P.g * (M.rho64[cq0 + sz * k] - P.rho_ref);
         Rd[1] += f;
         Rd[3] += f2d(tu[PL]) * f;
       }
@@ -339,38 +314,6 @@ __global__ void __launch_bounds__(TX * TY, 2)
       for (int w = 0; w < 4; ++w) {
         if (Rout) Rout[c + g.sv * w] = Rd[w];
         else Unew[c + g.sv * w] = uo[w] + coef * Rd[w];
-      }
-      if (ceq) {
-        const float* tr = tb + L.rho + pl.own;
-        const float* tn = tb + L.nrg + pl.own;
-        const float r12x = P.r12_f[0], r12y = P.r12_f[1], r12z = P.r12_f[2];
-        auto dx4 = [&](const float* a) { return (a[-2] - 8.0f * a[-1] + 8.0f * a[1] - a[2]) * r12x; };
-        auto dy4 = [&](const float* a) {
-          return (a[-2 * HX] - 8.0f * a[-HX] + 8.0f * a[HX] - a[2 * HX]) * r12y;
-        };
-        auto dz4 = [&](const float* w) { return (w[0] - 8.0f * w[1] + 8.0f * w[3] - w[4]) * r12z; };
-        const float dxr = dx4(tr), dyr = dy4(tr), dzr = dz4(rw);
-        const float dxe = dx4(tn), dye = dy4(tn), dze = dz4(ew);
-        const float divu = dx4(tu) + dy4(tu + PL) + dz4(ww);
-        const float rgrad = sqrtf(dxr * dxr + dyr * dyr + dzr * dzr);
-        const float dnednr = (dxr * dxe + dyr * dye + dzr * dze) * (dxr * dxr + dyr * dyr + dzr * dzr);
-        const bool ind = dnednr < 0.0f;
-        const float Gs[5] = {divu < 0.f && !ind ? rgrad : 0.f, ind ? rgrad : 0.f, dxr, dyr, dzr};
-        const float dxm = P.dxmag_f;
-        const float src = maxS / (P.eps_f * dxm);
-        const float dif = P.kap_f * maxS * dxm;
-#pragma unroll
-        for (int q = 0; q < 5; ++q) {
-          const float* tc = tb + L.c + q * PL + pl.own;
-          const float cc = tc[0];
-          const float lap = (tc[-1] - 2.0f * cc + tc[1]) * fc.rd[0] +
-                            (tc[-HX] - 2.0f * cc + tc[HX]) * fc.rd[1] +
-                            (cw[q][0] - 2.0f * cc + cw[q][2]) * fc.rd[2];
-          const double Rv = f2d(src * (Gs[q] - cc) + dif * lap);
-          const long long a = c + g.sv * (P.nv + q);
-          if (Rout) Rout[a] = Rv;
-          else Unew[a] = uo[4 + q] + coef * Rv;
-        }
       }
     }
     if (!__syncthreads_and(ok)) {
@@ -389,15 +332,215 @@ __global__ void __launch_bounds__(TX * TY, 2)
   }
 }
 
+// calculateRhoGrad + updateCeq (src/ceq3d.hpp:95-224): the shock and contact
+// switches take the signs of div u and of grad rho . grad e, so rho, e and
+// the velocity enter as FP32 pairs (hi parts from rho, nrg, vel; lo parts
+// from M.lo); the C variables and their Laplacian are FP32.  Cn (fused
+// stages): the next stage's FP32 C variables of U_new and, in red_n[1], the
+// interior maximum of |C_hat| of U_new.
+__global__ void __launch_bounds__(TX * TY, 2)
+    k_mceq3d(const __grid_constant__ Mixed3DMaps maps, Geo g, Geo gq, Phys P, MixedView M,
+             const unsigned long long* __restrict__ red, const double* Uold, double* Unew,
+             double coef, double* __restrict__ Rout, unsigned int* __restrict__ err,
+             float* __restrict__ Cn, unsigned long long* __restrict__ red_n) {
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  unsigned char* smraw = aligned_smem(smdyn);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
+  const CeqLayout L = ceq_layout();
+  float* tiles = reinterpret_cast<float*>(smraw + BAR_BYTES);
+  const int tid = threadIdx.y * TX + threadIdx.x;
+  const Place pl = place_cells(g);
+  const int i = pl.i, j = pl.j;
+  const int kc0 = g.ng + (int)blockIdx.z * KZ3;
+  const int kc1 = min(kc0 + KZ3, g.ngk - g.ng);
+  const bool cell = i < g.ngi - g.ng && j < g.ngj - g.ng;
+  const long long cq0 = (long long)i + gq.sy * j;
+  const long long c0 = (long long)i + g.sy * j;
+  const long long sz = gq.sz, qv = gq.sv;
+  float maxS;
+  const FaceCtx fc = make_ctx(P, red, &maxS);
+  if (tid == 0) {
+    prefetch_map(&maps.rho);
+    prefetch_map(&maps.lo4);
+    for (int q = 0; q < NBUF; ++q) mbar_init(&bar[q], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int m) {  // plane kc0 + m into buffer m % NBUF
+    const int buf = m % NBUF, k = kc0 + m;
+    float* tb = tiles + buf * L.size;
+    mbar_arrive_expect_tx(&bar[buf], L.bytes);
+    tma_load_4d(tb + L.v, &maps.v2, &bar[buf], pl.x0, pl.y0, k, 0);
+    tma_load_4d(tb + L.rho, &maps.rho, &bar[buf], pl.x0, pl.y0, k, 0);
+    tma_load_4d(tb + L.nrg, &maps.nrg, &bar[buf], pl.x0, pl.y0, k, 0);
+    tma_load_4d(tb + L.c, &maps.c5, &bar[buf], pl.x0, pl.y0, k, 0);
+    tma_load_4d(tb + L.lo, &maps.lo4, &bar[buf], pl.x0, pl.y0, k, 0);
+  };
+  if (tid == 0) {
+    issue(0);
+    if (kc0 + 1 < kc1) issue(1);
+  }
+  // own-column windows at planes k-2 .. k+2 (+ next) of the pairs of rho, e
+  // and w; C at k-1 .. k+1 (+ next)
+  const float* vz = M.vel + 2 * qv;
+  const float* rlo = M.lo;  // pair low parts: [0] rho, [1] e, [4] w
+  const float* elo = M.lo + qv;
+  const float* wlo = M.lo + 4 * qv;
+  float rw[5], rl[5], ew[5], el[5], ww[5], wl[5];
+  float rn = 0.f, rln = 0.f, en = 0.f, eln = 0.f, wn = 0.f, wln = 0.f;
+  float cw[5][3], cn[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    const long long o = cq0 + sz * (kc0 - 3 + m);  // planes kc0-3 .. kc0+1, shifted in below
+    rw[m] = cell ? M.rho[o] : 0.f;
+    rl[m] = cell ? rlo[o] : 0.f;
+    ew[m] = cell ? M.nrg[o] : 0.f;
+    el[m] = cell ? elo[o] : 0.f;
+    ww[m] = cell ? vz[o] : 0.f;
+    wl[m] = cell ? wlo[o] : 0.f;
+  }
+  if (cell) {
+    const long long o = cq0 + sz * (kc0 + 2);
+    rn = M.rho[o];
+    rln = rlo[o];
+    en = M.nrg[o];
+    eln = elo[o];
+    wn = vz[o];
+    wln = wlo[o];
+  }
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m) cw[q][m] = cell ? M.C[cq0 + qv * q + sz * (kc0 - 2 + m)] : 0.f;
+    cn[q] = cell ? M.C[cq0 + qv * q + sz * (kc0 + 1)] : 0.f;
+  }
+  // old state of the C variables, one plane ahead
+  double uo[5], un[5];
+  auto load_old = [&](int k, double* u) {
+    const long long c = c0 + g.sz * k;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) u[q] = Uold[c + g.sv * (P.nv + q)];
+  };
+  if (cell && !Rout) load_old(kc0, un);
+  float lC = -3.0e38f;
+
+  bool ok = true;
+  int k = kc0;
+  for (; k < kc1; ++k) {
+    const int n = k - kc0, b = n % NBUF;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      rw[m] = rw[m + 1];
+      rl[m] = rl[m + 1];
+      ew[m] = ew[m + 1];
+      el[m] = el[m + 1];
+      ww[m] = ww[m + 1];
+      wl[m] = wl[m + 1];
+    }
+    rw[4] = rn;
+    rl[4] = rln;
+    ew[4] = en;
+    el[4] = eln;
+    ww[4] = wn;
+    wl[4] = wln;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      cw[q][0] = cw[q][1];
+      cw[q][1] = cw[q][2];
+      cw[q][2] = cn[q];
+      uo[q] = un[q];
+    }
+    if (cell && k + 1 < kc1) {
+      const long long o = cq0 + sz * (k + 3);
+      rn = M.rho[o];
+      rln = rlo[o];
+      en = M.nrg[o];
+      eln = elo[o];
+      wn = vz[o];
+      wln = wlo[o];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) cn[q] = M.C[cq0 + qv * q + sz * (k + 2)];
+      if (!Rout) load_old(k + 1, un);
+    }
+    ok = ok && mbar_wait(&bar[b], (uint32_t)((n / NBUF) & 1), err);
+    if (cell && ok) {
+      const float* tb = tiles + b * L.size;
+      const float r12x = P.r12_f[0], r12y = P.r12_f[1], r12z = P.r12_f[2];
+      const float* tu = tb + L.v + pl.own;
+      const float* tr = tb + L.rho + pl.own;
+      const float* tn = tb + L.nrg + pl.own;
+      const float* tlo = tb + L.lo + pl.own;  // rho, e, u, v low parts
+      const float dxr = d4pair(tr, tlo, 1, r12x), dyr = d4pair(tr, tlo, HX, r12y);
+      const float dzr = d4pairz(rw, rl, r12z);
+      const float dxe = d4pair(tn, tlo + PL, 1, r12x), dye = d4pair(tn, tlo + PL, HX, r12y);
+      const float dze = d4pairz(ew, el, r12z);
+      const float divu = d4pair(tu, tlo + 2 * PL, 1, r12x) +
+                         d4pair(tu + PL, tlo + 3 * PL, HX, r12y) + d4pairz(ww, wl, r12z);
+      const float rg2 = dxr * dxr + dyr * dyr + dzr * dzr;
+      const float rgrad = sqrtf(rg2);
+      const float dnednr = (dxr * dxe + dyr * dye + dzr * dze) * rg2;
+      const bool ind = dnednr < 0.0f;
+      const float Gs[5] = {divu < 0.f && !ind ? rgrad : 0.f, ind ? rgrad : 0.f, dxr, dyr, dzr};
+      const float dxm = P.dxmag_f;
+      const float src = maxS / (P.eps_f * dxm);
+      const float dif = P.kap_f * maxS * dxm;
+      const long long c = c0 + g.sz * k;
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        const float* tc = tb + L.c + q * PL + pl.own;
+        const float cc = tc[0];
+        const float lap = (tc[-1] - 2.0f * cc + tc[1]) * fc.rd[0] +
+                          (tc[-HX] - 2.0f * cc + tc[HX]) * fc.rd[1] +
+                          (cw[q][0] - 2.0f * cc + cw[q][2]) * fc.rd[2];
+        const double Rv = f2d(src * (Gs[q] - cc) + dif * lap);
+        const long long a = c + g.sv * (P.nv + q);
+        if (Rout) {
+          Rout[a] = Rv;
+        } else {
+          const double unew = uo[q] + coef * Rv;
+          Unew[a] = unew;
+          if (Cn) {  // the next stage's FP32 C variables and max |C_hat|
+            const float cf = d2f(unew);
+            Cn[cq0 + sz * k + qv * q] = cf;
+            if (q == 1) lC = fmaxf(lC, fabsf(cf));
+          }
+        }
+      }
+    }
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0 && k + 2 < kc1) {
+      fence_proxy_async();
+      issue(n + 2);
+    }
+  }
+  if (Cn) {  // maxGradFunctor(var, nv+1) of U_new (src/ceq3d.hpp:82-93)
+    lC = warp_maxf(lC);
+    if ((tid & 31) == 0 && lC > -1e38f) atomicMax(&red_n[1], fst_key((double)lC));
+  }
+  if (!ok && tid == 0) {
+    for (int m = k - kc0; m <= k - kc0 + 1 && kc0 + m < kc1; ++m)
+      mbar_wait(&bar[m % NBUF], (uint32_t)((m / NBUF) & 1), err);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // k_mspec3d: species [sb, sb+nsk)
 // ---------------------------------------------------------------------------
-template <int NS, bool HYB>
-__global__ void __launch_bounds__(TX * TY, 3)
+// EPI (fused stages, all species in this launch): the kernel runs last in
+// the stage and, per cell, also evaluates the equation of state of U_new
+// (eos3: its new species from registers, momenta and energy as k_mmom3d left
+// them) into the next stage's primitive set On, and the wave-speed maximum
+// into red_n[0].
+template <int NS, bool HYB, bool EPI>
+__global__ void __launch_bounds__(TX * TY, EPI ? 2 : 3)
     k_mspec3d(const __grid_constant__ Mixed3DMaps maps, Geo g, Geo gq, Phys P, MixedView M,
               const unsigned char* __restrict__ smap, const double* Uold, double* Unew,
               double coef, double* __restrict__ Rout, int sb, int nsk,
-              unsigned int* __restrict__ err) {
+              unsigned int* __restrict__ err, Prim3Out On,
+              unsigned long long* __restrict__ red_n) {
   extern __shared__ __align__(128) unsigned char smdyn[];
   unsigned char* smraw = aligned_smem(smdyn);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
@@ -451,7 +594,8 @@ __global__ void __launch_bounds__(TX * TY, 3)
     for (int s = 0; s < NS; ++s) qz[s][m] = (in_arr && s < nsk) ? M.Q[o + gq.sv * (s0 + s)] : 0.f;
     wz[m] = in_arr ? vz[o] : 0.f;
   }
-  double uo[NS];
+  double uo[NS], um[4];
+  float lS = -3.0e38f;
 
   float Gz[NS], Gx[NS], Gy[NS];
 #pragma unroll
@@ -484,6 +628,10 @@ __global__ void __launch_bounds__(TX * TY, 3)
       const long long c = c0 + g.sz * k;
 #pragma unroll
       for (int s = 0; s < NS; ++s) uo[s] = s < nsk ? Uold[c + g.sv * (s0 + s)] : 0.0;
+      if (EPI) {
+#pragma unroll
+        for (int w = 0; w < 4; ++w) um[w] = Unew[c + g.sv * w];
+      }
     }
     ok = ok && mbar_wait(&bar[b], (uint32_t)((n / NBUF) & 1), err);
     const float* tb = tiles + b * L.size;
@@ -539,16 +687,30 @@ __global__ void __launch_bounds__(TX * TY, 3)
     }
     if (cell_col) {
       const long long c = c0 + g.sz * k;
+      double un[NS];
 #pragma unroll
       for (int s = 0; s < NS; ++s) {
         if (s >= nsk) break;
         const long long a = c + g.sv * (s0 + s);
-        if (Rout) Rout[a] = f2d(R[s]);
-        else Unew[a] = uo[s] + coef * f2d(R[s]);
+        if (Rout) {
+          Rout[a] = f2d(R[s]);
+        } else {
+          un[s] = uo[s] + coef * f2d(R[s]);
+          Unew[a] = un[s];
+        }
+      }
+      if (EPI) {
+        float sp;
+        eos3<NS>(P, un, um, On, cqk, gq.sv, &sp);
+        lS = fmaxf(lS, sp);
       }
     }
 #pragma unroll
     for (int s = 0; s < NS; ++s) Gz[s] = Gzn[s];
+  }
+  if (EPI) {  // interior maximum of |u| + c of U_new (maxWaveSpeed, src/ceq3d.hpp:25-63)
+    lS = warp_maxf(lS);
+    if ((tid & 31) == 0 && lS > -1e38f) atomicMax(&red_n[0], fst_key((double)lS));
   }
   if (!ok && tid == 0) {
     for (int m = k - kc0; m <= k - kc0 + 1 && kc0 + m < kc1; ++m)
@@ -886,23 +1048,37 @@ size_t mom_smem(bool visc, bool ceq) {
   return ALIGN_SLACK + BAR_BYTES +
          sizeof(float) * (NBUF * (size_t)L.tsize + NRING * (size_t)L.rsize + 2 * (size_t)TY * TX * 4);
 }
-size_t cell_smem(bool ceq) {
-  return ALIGN_SLACK + BAR_BYTES + sizeof(float) * NBUF * (size_t)cell_layout(ceq).size;
+size_t cell_smem() {
+  return ALIGN_SLACK + BAR_BYTES + sizeof(float) * NBUF * (size_t)cell_layout().size;
+}
+size_t ceq_smem() {
+  return ALIGN_SLACK + BAR_BYTES + sizeof(float) * NBUF * (size_t)ceq_layout().size;
 }
 
 template <int NS, bool HYB>
 int launch_spec(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
                 const unsigned char* smooth, const double* Uold, double* Unew, double coef,
-                double* Rout, cudaStream_t st) {
-  (void)P;
+                double* Rout, cudaStream_t st, bool fused) {
   const dim3 grd(cdiv3(g.nci, TX - 1), cdiv3(g.ncj, TY - 1), cdiv3(g.nck, KZ3));
   const size_t sm = spec_smem(NS);
-  cudaFuncSetAttribute(k_mspec3d<NS, HYB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (fused) {  // one launch over all species, with the equation-of-state epilogue
+    const PrimSet& A = b.alt;
+    const Prim3Out On{A.Q, A.rho32, A.vel32, A.p32, P.visc ? A.mu32 : nullptr,
+                      P.ceq ? A.nrg : nullptr, nullptr, P.ceq ? A.plo : nullptr, A.rho64};
+    cudaFuncSetAttribute(k_mspec3d<NS, HYB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_mspec3d<NS, HYB, true><<<grd, dim3(TX, TY), sm, st>>>(
+        *b.maps3d, g, b.gq, P, M, smooth, Uold, Unew, coef, Rout, 0, g.ns, b.dev_err, On, A.red);
+    return 1;
+  }
+  cudaFuncSetAttribute(k_mspec3d<NS, HYB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sm);
   int n = 0;
   for (int sb = 0; sb < g.ns; sb += NS) {
     const int nsk = g.ns - sb < NS ? g.ns - sb : NS;
-    k_mspec3d<NS, HYB><<<grd, dim3(TX, TY), sm, st>>>(*b.maps3d, g, b.gq, P, M, smooth, Uold,
-                                                      Unew, coef, Rout, sb, nsk, b.dev_err);
+    k_mspec3d<NS, HYB, false><<<grd, dim3(TX, TY), sm, st>>>(*b.maps3d, g, b.gq, P, M, smooth,
+                                                             Uold, Unew, coef, Rout, sb, nsk,
+                                                             b.dev_err, Prim3Out{}, nullptr);
     ++n;
   }
   return n;
@@ -911,13 +1087,13 @@ int launch_spec(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView
 template <bool HYB>
 int launch_spec_any(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
                     const unsigned char* smooth, const double* Uold, double* Unew, double coef,
-                    double* Rout, cudaStream_t st) {
+                    double* Rout, cudaStream_t st, bool fused) {
   switch (b.maps3d->nsc) {
-    case 1: return launch_spec<1, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st);
-    case 2: return launch_spec<2, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st);
-    case 3: return launch_spec<3, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st);
-    case 4: return launch_spec<4, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st);
-    default: return launch_spec<5, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st);
+    case 1: return launch_spec<1, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, fused);
+    case 2: return launch_spec<2, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, fused);
+    case 3: return launch_spec<3, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, fused);
+    case 4: return launch_spec<4, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, fused);
+    default: return launch_spec<5, HYB>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st, fused);
   }
 }
 
@@ -935,10 +1111,21 @@ void launch_mom(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView
 void launch_cell(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
                  const double* Uold, double* Unew, double coef, double* Rout, cudaStream_t st) {
   const dim3 grd(cdiv3(g.nci, TX), cdiv3(g.ncj, TY), cdiv3(g.nck, KZ3));
-  const size_t sm = cell_smem(P.ceq != 0);
+  const size_t sm = cell_smem();
   cudaFuncSetAttribute(k_mcell3d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_mcell3d<<<grd, dim3(TX, TY), sm, st>>>(*b.maps3d, g, b.gq, P, M, b.red, Uold, Unew, coef,
-                                          Rout, b.dev_err);
+  k_mcell3d<<<grd, dim3(TX, TY), sm, st>>>(*b.maps3d, g, b.gq, P, M, Uold, Unew, coef, Rout,
+                                          b.dev_err);
+}
+
+void launch_ceq(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
+                const double* Uold, double* Unew, double coef, double* Rout, cudaStream_t st,
+                bool fused) {
+  const dim3 grd(cdiv3(g.nci, TX), cdiv3(g.ncj, TY), cdiv3(g.nck, KZ3));
+  const size_t sm = ceq_smem();
+  cudaFuncSetAttribute(k_mceq3d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_mceq3d<<<grd, dim3(TX, TY), sm, st>>>(*b.maps3d, g, b.gq, P, M, b.red, Uold, Unew, coef,
+                                         Rout, b.dev_err, fused ? b.alt.C : nullptr,
+                                         fused ? b.alt.red : nullptr);
 }
 
 // species per k_mspec3d launch: all of them up to 5, else chunks of 4
@@ -995,59 +1182,92 @@ Geo fst_prim_geo(const Geo& g) {
   return q;
 }
 
+namespace {
+// tensor maps over one set of primitive arrays
+int build_maps(const Geo& g, const Geo& gq, const float* Q, const float* vel32, const float* p32,
+               const float* rho32, const float* nrg, const float* mu32, const float* C,
+               const float* plo, Mixed3DMaps** out, std::string* why) {
+  Mixed3DMaps* m = new (std::nothrow) Mixed3DMaps();
+  if (!m) return FST_ERR_OOM;
+  m->nsc = species_chunk(g.ns);
+  bool ok = make_map(&m->qs, g, gq, Q, g.nv, m->nsc, false, why) &&
+            make_map(&m->q4, g, gq, Q, g.nv, 4, false, why) &&
+            make_map(&m->v2, g, gq, vel32, 3, 2, false, why) &&
+            make_map(&m->v3, g, gq, vel32, 3, 3, false, why) &&
+            make_map(&m->p, g, gq, p32, 2, 2, false, why);
+  if (ok && rho32) ok = make_map(&m->rho, g, gq, rho32, 1, 1, false, why);
+  if (ok && nrg) ok = make_map(&m->nrg, g, gq, nrg, 1, 1, false, why);
+  if (ok && mu32) ok = make_map(&m->mu, g, gq, mu32, 1, 1, false, why);
+  if (ok && C) ok = make_map(&m->c5, g, gq, C, 5, 5, false, why) &&
+                    make_map(&m->c4, g, gq, C, 5, 4, false, why);
+  if (ok && plo) ok = make_map(&m->lo4, g, gq, plo, 5, 4, false, why);
+  if (!ok) {
+    delete m;
+    return FST_ERR_CUDA;
+  }
+  *out = m;
+  return FST_OK;
+}
+}  // namespace
+
 int fst_mixed3d_prepare(const Geo& g, MixedBufs& b, std::string* why) {
   if (g.ndim != 3) return FST_OK;
   if (g.ng != 3) {
     if (why) *why = "the 3D mixed kernels need ng = 3";
     return FST_ERR_UNSUPPORTED;
   }
-  Mixed3DMaps* m = new (std::nothrow) Mixed3DMaps();
-  if (!m) return FST_ERR_OOM;
-  const Geo& gq = b.gq;
-  m->nsc = species_chunk(g.ns);
-  bool ok = make_map(&m->qs, g, gq, b.Q, g.nv, m->nsc, false, why) &&
-            make_map(&m->q4, g, gq, b.Q, g.nv, 4, false, why) &&
-            make_map(&m->v2, g, gq, b.vel32, 3, 2, false, why) &&
-            make_map(&m->v3, g, gq, b.vel32, 3, 3, false, why) &&
-            make_map(&m->p, g, gq, b.p32, 2, 2, false, why);
-  if (ok && b.rho32) ok = make_map(&m->rho, g, gq, b.rho32, 1, 1, false, why);
-  if (ok && b.nrg) ok = make_map(&m->nrg, g, gq, b.nrg, 1, 1, false, why);
-  if (ok && b.mu32) ok = make_map(&m->mu, g, gq, b.mu32, 1, 1, false, why);
-  if (ok && b.C) ok = make_map(&m->c5, g, gq, b.C, 5, 5, false, why) &&
-                      make_map(&m->c4, g, gq, b.C, 5, 4, false, why);
-  if (!ok) {
-    delete m;
-    return FST_ERR_CUDA;
+  int rc = build_maps(g, b.gq, b.Q, b.vel32, b.p32, b.rho32, b.nrg, b.mu32, b.C, b.plo,
+                      &b.maps3d, why);
+  if (rc == FST_OK && b.fused) {
+    const PrimSet& A = b.alt;
+    rc = build_maps(g, b.gq, A.Q, A.vel32, A.p32, A.rho32, A.nrg, A.mu32, A.C, A.plo,
+                    &b.alt.maps3d, why);
   }
-  b.maps3d = m;
-  return FST_OK;
+  return rc;
 }
 
 void fst_mixed3d_release(MixedBufs& b) {
   delete b.maps3d;
   b.maps3d = nullptr;
+  delete b.alt.maps3d;
+  b.alt.maps3d = nullptr;
 }
 
 int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
                     const unsigned char* smooth, const double* Uold, double* Unew, double coef,
-                    double* Rout, cudaStream_t st, Prof* prof, bool hybrid) {
+                    double* Rout, cudaStream_t st, Prof* prof, bool hybrid, bool fused) {
   int n = 0;
   // cell terms first: k_mmom3d adds its face terms to what k_mcell3d wrote
   // (on a generalized grid, the metric pressure gradient)
-  if (b.metf)
+  if (b.metf) {
     FST_LAUNCH(prof, "gen_cell", st, n,
                fst_mixedgen_cell(g, b.gq, M, b.metf, Uold, Unew, coef, Rout, st));
-  else
+  } else {
     FST_LAUNCH(prof, "mcell3d", st, n, launch_cell(g, P, b, M, Uold, Unew, coef, Rout, st));
-  if (hybrid) {
-    FST_LAUNCH(prof, "mspec3d_hybrid", st, n,
-               n += launch_spec_any<true>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st) - 1);
+    if (P.ceq)
+      FST_LAUNCH(prof, "mceq3d", st, n,
+                 launch_ceq(g, P, b, M, Uold, Unew, coef, Rout, st, fused));
+  }
+  // fused stages: the species kernel runs last, after the momenta and energy
+  // of U_new are complete, and evaluates the next stage's primitives
+  auto spec = [&]() {
+    const char* nm = fused ? (hybrid ? "mspec3d_hybrid_eos" : "mspec3d_eos")
+                           : (hybrid ? "mspec3d_hybrid" : "mspec3d");
+    if (hybrid)
+      FST_LAUNCH(prof, nm, st, n,
+                 n += launch_spec_any<true>(g, P, b, M, smooth, Uold, Unew, coef, Rout, st,
+                                            fused) - 1);
+    else
+      FST_LAUNCH(prof, nm, st, n,
+                 n += launch_spec_any<false>(g, P, b, M, nullptr, Uold, Unew, coef, Rout, st,
+                                             fused) - 1);
+  };
+  if (!fused) spec();
+  if (hybrid)
     FST_LAUNCH(prof, "mmom3d_hybrid", st, n,
                launch_mom<true>(g, P, b, M, smooth, Unew, coef, Rout, st));
-  } else {
-    FST_LAUNCH(prof, "mspec3d", st, n,
-               n += launch_spec_any<false>(g, P, b, M, nullptr, Uold, Unew, coef, Rout, st) - 1);
+  else
     FST_LAUNCH(prof, "mmom3d", st, n, launch_mom<false>(g, P, b, M, nullptr, Unew, coef, Rout, st));
-  }
+  if (fused) spec();
   return n;
 }

@@ -54,6 +54,67 @@ __device__ __forceinline__ double rcp64(double x) {
   return fma(r, fma(-x, r, 1.0), r);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 pairs ("double-float"): a value carried as h + l with |l| at most
+// about ulp(h), ~48 significant bits.  GB300 retires FP64 instructions at
+// 1/64 of the FP32 rate, so quantities that need more than FP32 accuracy are
+// formed with error-free transformations on the FP32 pipe instead: Knuth's
+// TwoSum, the FMA TwoProduct, and Dekker's double-length sum, product and
+// quotient (Dekker 1971).  The rounded operations are written as intrinsics
+// so that no contraction or fast-math rewrite can change them.
+// ---------------------------------------------------------------------------
+struct f2p {
+  float h, l;
+};
+__device__ __forceinline__ f2p two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ f2p fast_two_sum(float a, float b) {  // |a| >= |b| or a = 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ f2p df_add(f2p a, f2p b) {
+  const f2p s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ f2p df_mul(f2p a, f2p b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);  // a.h * b.h = p + e exactly
+  e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ f2p df_div(f2p a, f2p b) {
+  const float r = __frcp_rn(b.h);
+  const float q = __fmul_rn(a.h, r);
+  const float p = __fmul_rn(q, b.h);
+  const float pe = __fmaf_rn(q, b.h, -p);  // q * b.h = p + pe exactly
+  // remainder a - q*b: a.h - p is exact (p is within a factor 2 of a.h)
+  float rem = __fsub_rn(__fsub_rn(a.h, p), pe);
+  rem = __fadd_rn(rem, __fmaf_rn(-q, b.l, a.l));
+  return fast_two_sum(q, __fmul_rn(rem, r));
+}
+// x - d2f(x) as an FP32 number, by integer operations on the bits of x (no
+// FP64 instruction).  d2f keeps the top 23 mantissa bits and rounds on the
+// 29 it drops (D); the remainder is D * 2^(E-52), less 2^(E-23) when d2f
+// rounded up, E the unbiased exponent of x.  It is formed exactly as
+// F - B with B = 2^(E-23) and F = B * (1 + D / 2^29) (the 6 lowest bits of D
+// truncated: 2^-46 relative to x).  Zero when x is zero, non-finite, or so
+// small (|x| < 2^-103) or large (beyond FP32) that the pair has no low part.
+__device__ __forceinline__ float lo_part(double x) {
+  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+  const unsigned int ex = (hi >> 20) & 0x7FFu;
+  const unsigned int sg = hi & 0x80000000u;
+  const unsigned int ef = (ex - 919u) << 23;  // FP32 exponent field of 2^(E-23)
+  const float B = __uint_as_float(sg | ef);
+  const float F = __uint_as_float(sg | ef | ((lo & 0x1FFFFFFFu) >> 6));
+  float r = __fsub_rn(F, B);
+  r = ((lo >> 28) & 1u) ? __fsub_rn(r, B) : r;
+  return (ex < 920u || ex > 1150u) ? 0.0f : r;
+}
+__device__ __forceinline__ f2p split(double x) { return {d2f(x), lo_part(x)}; }
+
 __device__ __forceinline__ float warp_maxf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -149,6 +210,124 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
       else sp = sqrtf(Cp2 / Cv2 * pf * rif) + mf;  // maxWaveSpeed2D quirks
       lS = fmaxf(lS, sp);
       lC = fmaxf(lC, fabsf(Cc[q + qv]));
+    }
+  }
+}
+
+// Outputs of the 3D primitive pass (primitive layout gq).  lo, when set
+// (C-equation runs), receives the low parts of five FP32 pairs: [0] rho,
+// [1] the C-equation internal energy, [2..4] u, v, w; their high parts are
+// rho, nrg and vel.  rho64 (buoyancy) receives the density as an FP64 value.
+struct Prim3Out {
+  float *Q, *rho, *vel, *pp, *mu, *nrg, *C, *lo;
+  double* rho64;
+};
+
+// The 3D equation of state with no FP64 instruction, in FP32 pairs.  The
+// state values enter as pairs (d2f + lo_part); the density rho = sum rho_s,
+// the mixture sums sum rho_s cv_s and sum rho_s R_s, gamma - 1 = their
+// quotient and p = (gamma-1)(E - KE) (calculateRhoPT3D,
+// src/secondary.hpp:109-151) carry ~48 bits, the accuracy the pressure
+// gradient needs where it is a small difference of large pressures.  KE is
+// FP32, as in mprim_cell.  The velocity u = m/rho (computeVelocity3D,
+// src/velocity.hpp:68-83) and the C-equation energy nrg = E/rho -
+// 0.5*rho*|u|^2 (calculateRhoGrad, src/ceq3d.hpp:138-141; rho*|u|^2 formed as
+// |m|^2/rho) are pairs as well: the shock and contact switches of updateCeq
+// take the signs of products of their derivatives, and FP32 rounding of the
+// values alone flips them wherever a derivative is small against the value.
+//
+// eos3: one cell from its FP64 state values (species us[0..ns), momenta
+// um[0..2], energy um[3]), written to O at primitive index q (field stride
+// qv); returns the cell's wave speed |u| + c in *sp.  NS: the species count
+// when it is known at compile time (every loop then unrolls), 0 for any.
+template <int NS>
+__device__ __forceinline__ void eos3(const Phys& P, const double* us, const double um[4],
+                                     const Prim3Out& O, long long q, long long qv, float* sp) {
+  f2p r = {0.f, 0.f}, cv = {0.f, 0.f}, rm = {0.f, 0.f};
+  float msum = 0.f;
+  const int ns = NS > 0 ? NS : P.ns;
+#pragma unroll
+  for (int s = 0; s < (NS > 0 ? NS : FST_MAX_SPECIES); ++s) {
+    if (NS == 0 && s >= ns) break;
+    const f2p a = split(us[s]);
+    O.Q[q + qv * (4 + s)] = a.h;
+    r = df_add(r, a);
+    cv = df_add(cv, df_mul(a, f2p{P.cv_f[s], P.cv_lf[s]}));
+    rm = df_add(rm, df_mul(a, f2p{P.rm_f[s], P.rm_lf[s]}));
+    msum = fmaf(a.h, P.mu_f[s], msum);
+  }
+  const float rif = __frcp_rn(r.h);
+  if (O.mu) O.mu[q] = msum * rif;  // sum_s Y_s mu_s
+  f2p m[3];
+  float msq = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    m[d] = split(um[d]);
+    O.Q[q + qv * d] = m[d].h;
+    msq = fmaf(m[d].h, m[d].h, msq);
+    const f2p u = df_div(m[d], r);
+    O.vel[q + qv * d] = u.h;
+    if (O.lo) O.lo[q + qv * (2 + d)] = u.l;
+  }
+  const f2p E = split(um[3]);
+  const f2p gm1 = df_div(rm, cv);
+  const f2p p = df_mul(gm1, df_add(E, f2p{-0.5f * msq * rif, 0.f}));
+  O.pp[q] = p.h;
+  O.pp[q + qv] = p.l;
+  O.Q[q + qv * 3] = E.h + p.h;  // E + p, the energy's advected quantity
+  O.rho[q] = r.h;
+  if (O.rho64) O.rho64[q] = f2d(r.h) + f2d(r.l);
+  if (O.nrg) {
+    f2p m2 = df_mul(m[0], m[0]);
+    m2 = df_add(m2, df_mul(m[1], m[1]));
+    m2 = df_add(m2, df_mul(m[2], m[2]));
+    const f2p kq = df_div(m2, r);  // rho |u|^2
+    const f2p e = df_add(df_div(E, r), f2p{-0.5f * kq.h, -0.5f * kq.l});
+    O.nrg[q] = e.h;
+    if (O.lo) {
+      O.lo[q] = r.l;
+      O.lo[q + qv] = e.l;
+    }
+  }
+  *sp = sqrtf((1.0f + gm1.h) * p.h * rif) + sqrtf(msq) * rif;
+}
+
+// One cell of the 3D primitive pass: loads the cell's state (every value
+// before any is used, so a thread has all its loads in flight at once),
+// writes the equation of state (eos3) and the FP32 C variables, and
+// accumulates the interior maxima of the wave speed and |C_hat| when `red`
+// is set.
+template <int NS>
+__device__ __forceinline__ void mprim3_cell(const Geo& g, const Geo& gq, const Phys& P,
+                                            const double* __restrict__ U, const Prim3Out& O,
+                                            bool red, int i, int j, int k, float& lS, float& lC) {
+  const long long sv = g.sv, qv = gq.sv;
+  const long long c = (long long)i + g.sy * j + g.sz * k;
+  const long long q = (long long)i + gq.sy * j + gq.sz * k;
+  double us[NS > 0 ? NS : FST_MAX_SPECIES], um[4], uc[5];
+#pragma unroll
+  for (int s = 0; s < (NS > 0 ? NS : FST_MAX_SPECIES); ++s) {
+    if (NS == 0 && s >= P.ns) break;
+    us[s] = U[c + sv * (4 + s)];
+  }
+#pragma unroll
+  for (int d = 0; d < 4; ++d) um[d] = U[c + sv * d];
+  if (O.C) {
+#pragma unroll
+    for (int n = 0; n < 5; ++n) uc[n] = U[c + sv * (P.nv + n)];
+  }
+  float sp;
+  eos3<NS>(P, us, um, O, q, qv, &sp);
+  if (O.C) {
+#pragma unroll
+    for (int n = 0; n < 5; ++n) O.C[q + qv * n] = d2f(uc[n]);
+  }
+  if (red) {
+    const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
+                    k >= g.ng && k < g.ngk - g.ng;
+    if (in) {
+      lS = fmaxf(lS, sp);
+      lC = fmaxf(lC, fabsf(d2f(uc[1])));
     }
   }
 }
