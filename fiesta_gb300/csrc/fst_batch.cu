@@ -41,7 +41,7 @@ struct BCase {
   double *Ua, *Ub;
   unsigned long long* red;  // 2 keys
   float* Q;                 // writable views of the mixed buffers
-  float *rho32, *vel32, *T32, *nrg, *C;
+  float *rho32, *vel32, *T32, *nrg, *C, *lo;
   double *p64, *rho64;
   int bc[4];     // xmin, xmax, ymin, ymax
   int per[2];    // x, y periodic
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) k_bprim(const BCase* __restrict__ cs,
   if (local < (int)g.sv) {
     const int i = local % g.ngi, j = local / g.ngi;
     mprim_cell<2>(g, g, Ps[c], use_a ? B.Ua : B.Ub, B.Q, B.rho32, B.rho64, B.vel32, B.p64, nullptr, nullptr,
-                  B.nrg, B.C, B.T32, red, i, j, 0, lS, lC);
+                  B.nrg, B.C, B.T32, B.lo, red, i, j, 0, lS, lC);
   }
   if (red) {
     lS = warp_maxf(lS);
@@ -381,8 +381,9 @@ int fst_batch_create(const fst_config* cfgs, int ncases, fst_batch** out) {
     if (cf.ceq) {
       A((void**)&B.nrg, sizeof(float) * n);
       A((void**)&B.C, sizeof(float) * n * 5);
+      A((void**)&B.lo, sizeof(float) * n * 4);
     }
-    B.M = MixedView{B.Q, B.rho32, B.vel32, B.p64, nullptr, B.nrg, B.C, B.T32, B.rho64};
+    B.M = MixedView{B.Q, B.rho32, B.vel32, B.p64, nullptr, B.nrg, B.C, B.T32, B.rho64, nullptr, B.lo};
     B.bc[0] = cf.bc_xmin;
     B.bc[1] = cf.bc_xmax;
     B.bc[2] = cf.bc_ymin;

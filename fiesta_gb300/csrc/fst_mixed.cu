@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const doub
                                                float* __restrict__ pp,
                                                float* __restrict__ mu, float* __restrict__ nrg,
                                                float* __restrict__ Cc, float* __restrict__ T,
+                                               float* __restrict__ lo,
                                                unsigned long long* __restrict__ red) {
   // grid: x runs over the cells of one (i, j) plane in storage order, in
   // blocks of 256 across row ends (streaming, no idle threads), z = k
@@ -47,7 +48,7 @@ __global__ void __launch_bounds__(256) k_mprim(Geo g, Geo gq, Phys P, const doub
   const int j = t / g.ngi, i = t - j * g.ngi;
   float lS = -3.0e38f, lC = -3.0e38f;
   if (j < g.ngj)
-    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red != nullptr, i, j,
+    mprim_cell<NDIM>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, lo, red != nullptr, i, j,
                      blockIdx.z, lS, lC);
   if (red) {
     lS = warp_maxf(lS);
@@ -151,9 +152,11 @@ inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 template <int NDIM>
 void launch_mprim(const Geo& g, const Geo& gq, const Phys& P, const double* U, float* Q,
                   float* rho, double* rho64, float* vel, double* pr, float* pp, float* mu,
-                  float* nrg, float* Cc, float* T, unsigned long long* red, cudaStream_t st) {
+                  float* nrg, float* Cc, float* T, float* lo, unsigned long long* red,
+                  cudaStream_t st) {
   const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
-  k_mprim<NDIM><<<qg, qb, 0, st>>>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, red);
+  k_mprim<NDIM><<<qg, qb, 0, st>>>(g, gq, P, U, Q, rho, rho64, vel, pr, pp, mu, nrg, Cc, T, lo,
+                                   red);
 }
 
 Prim3Out prim3_out(const Phys& P, const MixedBufs& b, bool all_outputs) {
@@ -248,7 +251,7 @@ int fst_mixed_alloc(const fst_config& cf, const Geo& g, MixedBufs& b, const fst_
   if (cf.ceq) {
     A((void**)&b.nrg, sizeof(float) * n);
     A((void**)&b.C, sizeof(float) * n * 5);
-    if (g.ndim == 3) A((void**)&b.plo, sizeof(float) * n * 5);
+    A((void**)&b.plo, sizeof(float) * n * 5);
   }
   A((void**)&b.rho, sizeof(double) * ns);
   A((void**)&b.pr, sizeof(double) * ns);
@@ -351,7 +354,8 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     FST_LAUNCH(prof, "mprim2d", st, n,
                launch_mprim<2>(g, b.gq, P, Uin, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr,
                                nullptr, P.ceq ? b.nrg : nullptr, P.ceq ? b.C : nullptr,
-                               P.visc ? b.T32 : nullptr, P.ceq ? b.red : nullptr, st));
+                               P.visc ? b.T32 : nullptr, P.ceq ? b.plo : nullptr,
+                               P.ceq ? b.red : nullptr, st));
   }
   bool hyb = cf.mode == FST_MODE_HYBRID && b.hyb_active;
   const unsigned char* smooth = b.smooth;
@@ -413,7 +417,7 @@ int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const Mix
     launch_mprim3(g, P, b, U, true, nullptr, st);
   else
     launch_mprim<2>(g, b.gq, P, U, b.Q, b.rho32, b.rho64, b.vel32, b.p64, nullptr, nullptr, b.nrg,
-                    b.C, b.T32, nullptr, st);
+                    b.C, b.T32, b.plo, nullptr, st);
   return 1;
 }
 

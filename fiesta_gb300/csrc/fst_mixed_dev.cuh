@@ -142,8 +142,8 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
                                            float* __restrict__ vel, double* __restrict__ pr,
                                            float* __restrict__ pp, float* __restrict__ mu,
                                            float* __restrict__ nrg, float* __restrict__ Cc,
-                                           float* __restrict__ T, bool red, int i, int j, int k,
-                                           float& lS, float& lC) {
+                                           float* __restrict__ T, float* __restrict__ lo,
+                                           bool red, int i, int j, int k, float& lS, float& lC) {
   const long long sv = g.sv, qv = gq.sv;
   const long long c = (long long)i + g.sy * j + g.sz * k;
   const long long q = (long long)i + gq.sy * j + gq.sz * k;
@@ -198,6 +198,28 @@ __device__ __forceinline__ void mprim_cell(const Geo& g, const Geo& gq, const Ph
   if (rho64) rho64[q] = r64;
   if (T) T[q] = d2f(p) / d2f(sRm);  // p / (rho R_mix), R_mix = sum rho_s R_s / rho
   if (nrg) nrg[q] = d2f(E) * rif - 0.5f * rf * usq;  // E/rho - 0.5*rho*|u|^2 (reference)
+  if (lo) {
+    // C-equation runs: rho, the velocity and nrg as FP32 pairs (high parts
+    // replace the FP32 values above), for the shock and contact switches;
+    // lo = [rho, nrg, u, v] low parts (see Prim3Out)
+    f2p r = {0.f, 0.f};
+    for (int s = 0; s < P.ns; ++s) r = df_add(r, split(U[c + sv * (s0 + s)]));
+    f2p m2 = {0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+      const f2p md = split(U[c + sv * d]);
+      const f2p u = df_div(md, r);
+      vel[q + qv * d] = u.h;
+      lo[q + qv * (2 + d)] = u.l;
+      m2 = df_add(m2, df_mul(md, md));
+    }
+    const f2p kq = df_div(m2, r);  // rho |u|^2
+    const f2p e = df_add(df_div(split(E), r), f2p{-0.5f * kq.h, -0.5f * kq.l});
+    rho[q] = r.h;
+    lo[q] = r.l;
+    nrg[q] = e.h;
+    lo[q + qv] = e.l;
+  }
   if (Cc)
     for (int n = 0; n < 5; ++n) Cc[q + qv * n] = d2f(U[c + sv * (P.nv + n)]);
   if (red) {
@@ -544,12 +566,18 @@ __device__ __forceinline__ void rhs2d_tile(const Geo& g, const Phys& P, const Mi
   }
   if (P.ceq) {
     const float r12x = P.r12_f[0], r12y = P.r12_f[1];
-    auto d4 = [&](const float* a, long long st, float r12) {
-      return (a[c - 2 * st] - 8.0f * a[c - st] + 8.0f * a[c + st] - a[c + 2 * st]) * r12;
+    // the switches take the signs of div u and grad rho . grad e: rho, e and
+    // the velocity enter as FP32 pairs (high parts M.rho / M.nrg / M.vel,
+    // low parts M.lo), differenced high with high and low with low
+    auto d4 = [&](const float* a, const float* l, long long st, float r12) {
+      const float d1 = (a[c + st] - a[c - st]) + (l[c + st] - l[c - st]);
+      const float d2 = (a[c + 2 * st] - a[c - 2 * st]) + (l[c + 2 * st] - l[c - 2 * st]);
+      return (8.0f * d1 - d2) * r12;
     };
-    const float dxr = d4(M.rho, 1, r12x), dyr = d4(M.rho, sy, r12y);
-    const float dxe = d4(M.nrg, 1, r12x), dye = d4(M.nrg, sy, r12y);
-    const float divu = d4(M.vel, 1, r12x) + d4(M.vel + sv, sy, r12y);
+    const float* lo = M.lo;
+    const float dxr = d4(M.rho, lo, 1, r12x), dyr = d4(M.rho, lo, sy, r12y);
+    const float dxe = d4(M.nrg, lo + sv, 1, r12x), dye = d4(M.nrg, lo + sv, sy, r12y);
+    const float divu = d4(M.vel, lo + 2 * sv, 1, r12x) + d4(M.vel + sv, lo + 3 * sv, sy, r12y);
     const float rgrad = sqrtf(dxr * dxr + dyr * dyr);
     const float dnednr = (dxr * dxe + dyr * dye) * (dxr * dxr + dyr * dyr);
     const bool i1 = dnednr < 0.0f;

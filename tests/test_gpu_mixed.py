@@ -1,26 +1,28 @@
 """Accuracy of the mixed-precision path (FP32 fluxes / viscous / C-equation,
-FP64 state, pressure recovery and RK combine) against the FP64 oracle.
+FP64 state, FP32-pair equation of state and RK combine) against the FP64
+oracle.
 
-Tolerances (relative L2 per conserved field over the interior):
-  state after N steps          <= 1e-5   (the mixed-precision target), for
-                                         fields that are not zero initially
-  state increment U_N - U_0    <= 2e-3   (the change the RHS produced), for
-                                         every field; for a field that starts
-                                         at zero (momenta at rest, C
-                                         variables) this is its whole value
+Every state field is judged, by relative L2 over the interior after N steps:
+the state itself where the field starts nonzero, else its increment (its
+whole value: momenta at rest, the C-equation variables).  The bar is 1e-5
+for all of them, with one exception: C, the shock sensor, follows the sign of
+div u in cells where div u is zero up to rounding, so two FP64 builds of the
+reference's own algorithm that differ only in fused multiply-adds already
+disagree on it by more than 1e-5 (oracle/oracle.py build_fma).  C is held to
+max(1e-5, 4 x that FP64 build-to-build spread), measured in the same test.
 """
 import numpy as np
 import pytest
 
 from fiesta_gb300 import abi
 from fiesta_gb300.solver import Solver, initial_conditions
-from oracle.oracle import Oracle
+from oracle.oracle import Oracle, OracleFMA
 from tests.golden_io import interior, rel_l2
 
 pytestmark = pytest.mark.gpu
 
 STATE_TOL = 1e-5
-INCR_TOL = 2e-3
+C_SPREAD_FACTOR = 4.0
 
 SP5 = [dict(gamma=g, M=m / 1000.0, mu=mu) for g, m, mu in
        zip([1.4, 1.67, 1.3, 1.32, 1.4], [28.96, 4.0, 44.0, 16.0, 2.0],
@@ -28,27 +30,44 @@ SP5 = [dict(gamma=g, M=m / 1000.0, mu=mu) for g, m, mu in
 
 
 def field_errors(cfg, U, Uref, U0):
-    """(v, state error or 0 for zero-initial fields, increment error)."""
-    nv = abi.nv_of(cfg)
+    """[(v, rel-L2)] for every state field (state-relative where the field
+    starts nonzero, else of its increment)."""
     out = []
-    for v in range(nv):
+    for v in range(U.shape[3]):
         a, b, z = interior(cfg, U[..., v]), interior(cfg, Uref[..., v]), interior(cfg, U0[..., v])
-        st = rel_l2(a, b) if np.abs(z).max() > 0 else 0.0
-        inc = rel_l2(a - z, b - z) if np.abs(b - z).max() > 0 else 0.0
-        out.append((v, st, inc))
+        if np.abs(z).max() > 0:
+            out.append((v, rel_l2(a, b)))
+        else:
+            out.append((v, rel_l2(a - z, b - z) if np.abs(b - z).max() > 0 else 0.0))
     return out
 
 
 def run_pair(cfg, U0, steps):
+    """Mixed-path state, the FP64 oracle's, and the FMA-built oracle's after
+    `steps` steps from U0."""
     m = Solver(cfg)
     m.set_state(U0)
     m.rk_step(steps)
     cref = abi.config_from_dict(abi.config_to_dict(cfg))
     cref.mode = abi.MODE_PLAIN_FP64
-    o = Oracle(cref)
-    o.set_state(U0)
-    o.rk_step(steps)
-    return m.get_state(), o.get_state()
+    out = [m.get_state()]
+    m.close()
+    for cls in (Oracle, OracleFMA):
+        o = cls(cref)
+        o.set_state(U0)
+        o.rk_step(steps)
+        out.append(o.get_state())
+    return out
+
+
+def check_fields(cfg, U, Ur, Uf, U0):
+    nv = abi.nv_of(cfg)
+    spread = dict(field_errors(cfg, Uf, Ur, U0))
+    for v, e in field_errors(cfg, U, Ur, U0):
+        tol = STATE_TOL
+        if cfg.ceq and v == nv:  # C, the shock sensor (see the module docstring)
+            tol = max(STATE_TOL, C_SPREAD_FACTOR * spread[v])
+        assert e <= tol, (v, e, tol)
 
 
 def mixing(n, dt, mode=abi.MODE_MIXED):
@@ -60,10 +79,7 @@ def test_mixed_mixing_3d_vs_oracle():
     cfg = mixing((48, 40, 32), dt=2e-7)
     U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 20261206, p_ambient=1e5, T_ambient=300.0,
                             nkernels=8)
-    U, Ur = run_pair(cfg, U0, 10)
-    for v, st, inc in field_errors(cfg, U, Ur, U0):
-        assert st <= STATE_TOL, (v, st)
-        assert inc <= INCR_TOL, (v, inc)
+    check_fields(cfg, *run_pair(cfg, U0, 10), U0)
 
 
 def test_mixed_expansion_3d_vs_oracle():
@@ -71,10 +87,7 @@ def test_mixed_expansion_3d_vs_oracle():
                           mode=abi.MODE_MIXED)
     U0 = initial_conditions(cfg, abi.IC_EXPANSION_3D, 20261204, p_ambient=1e5, T_ambient=300.0,
                             p_high=1e7, radius=0.1 * 32 / 32, noise=0.01)
-    U, Ur = run_pair(cfg, U0, 10)
-    for v, st, inc in field_errors(cfg, U, Ur, U0):
-        assert st <= STATE_TOL, (v, st)
-        assert inc <= INCR_TOL, (v, inc)
+    check_fields(cfg, *run_pair(cfg, U0, 10), U0)
 
 
 @pytest.mark.parametrize("case", ["sod", "rt"])
@@ -93,10 +106,7 @@ def test_mixed_2d_vs_oracle(case):
                               bcs=("outflow", "outflow", "hydrostatic", "hydrostatic", "outflow",
                                    "outflow"), mode=abi.MODE_MIXED)
         U0 = initial_conditions(cfg, abi.IC_RT_2D, 7, rho_heavy=2.0, rho_light=1.0, p_ambient=2.4)
-    U, Ur = run_pair(cfg, U0, 50)
-    for v, st, inc in field_errors(cfg, U, Ur, U0):
-        assert st <= STATE_TOL, (v, st)
-        assert inc <= INCR_TOL, (v, inc)
+    check_fields(cfg, *run_pair(cfg, U0, 50), U0)
 
 
 def test_mixed_rhs_close_to_oracle():
@@ -110,12 +120,11 @@ def test_mixed_rhs_close_to_oracle():
     o = Oracle(cref)
     o.set_state(U0)
     Ro = o.compute_rhs()
-    nv = abi.nv_of(cfg)
+    # one RHS evaluation: FP32 face terms (the increments' relative error),
+    # FP32-pair switches of the C-equation sources
     for v in range(abi.dims(cfg)[3]):
         e = rel_l2(interior(cfg, R[..., v]), interior(cfg, Ro[..., v]))
-        # the C-equation sources switch on sign tests of FP32 gradient
-        # products (src/ceq3d.hpp:160-176), so single cells may flip
-        assert e <= (1e-3 if v < nv else 5e-2), (v, e)
+        assert e <= 1e-3, (v, e)
 
 
 def test_mixed_many_species_fallback():
@@ -124,9 +133,7 @@ def test_mixed_many_species_fallback():
     cfg = abi.make_config(3, (12, 10, 9), dt=1e-4, species=sp, R=1.0, visc=True, ceq=True,
                           mode=abi.MODE_MIXED)
     U0 = initial_conditions(cfg, abi.IC_RANDOM_SMOOTH, 3)
-    U, Ur = run_pair(cfg, U0, 5)
-    for v, st, inc in field_errors(cfg, U, Ur, U0):
-        assert st <= STATE_TOL, (v, st)
+    check_fields(cfg, *run_pair(cfg, U0, 5), U0)
 
 
 @pytest.mark.parametrize("ns,visc,ceq,buoy", [(1, False, False, False), (3, True, False, True),
@@ -143,10 +150,7 @@ def test_mixed_3d_term_combinations_ragged_tiles(ns, visc, ceq, buoy):
                           mode=abi.MODE_MIXED)
     U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 11 + ns, p_ambient=1e5, T_ambient=300.0,
                             nkernels=4)
-    U, Ur = run_pair(cfg, U0, 6)
-    for v, st, inc in field_errors(cfg, U, Ur, U0):
-        assert st <= STATE_TOL, (v, st)
-        assert inc <= INCR_TOL, (v, inc)
+    check_fields(cfg, *run_pair(cfg, U0, 6), U0)
 
 
 @pytest.mark.parametrize("case", ["3d", "2d", "gen3d", "hybrid3d"])
