@@ -579,6 +579,10 @@ def accuracy_report(cfg, U0, finals, nsteps):
 
     out = {"steps": nsteps}
     pairs = [(m, "plain") for m in ("mixed", "hybrid") if m in finals and "plain" in finals]
+    if "plain_perturbed" in finals and "plain" in finals:
+        # the condition spread: how far the FP64 path itself moves when its
+        # initial state is perturbed by COND_EPS (relative, seeded)
+        pairs.insert(0, ("plain_perturbed", "plain"))
     if "hybrid" in finals and "mixed" in finals:
         pairs.append(("hybrid", "mixed"))
     for a_, b_ in pairs:
@@ -590,6 +594,30 @@ def accuracy_report(cfg, U0, finals, nsteps):
             else:
                 rows[name + " (increment)"] = rel(I(finals[a_], v) - z, I(finals[b_], v) - z)
         out[f"{a_}_vs_{b_}"] = rows
+    return out
+
+
+COND_EPS = 1e-9      # relative perturbation of the initial state (condition spread)
+COND_FACTOR = 10.0   # a field passes at max(1e-5, COND_FACTOR * its condition spread)
+
+
+def perturbed(U0, eps=COND_EPS, seed=1):
+    rng = np.random.default_rng(seed)
+    U = U0.copy()
+    nz = np.abs(U0) > 0
+    U[nz] *= 1 + eps * rng.standard_normal(int(nz.sum()))
+    return np.asfortranarray(U)
+
+
+def plain_final(n, U, dt, nsteps):
+    """State of the plain FP64 path (bit-identical to the reference's
+    arithmetic) after nsteps from U."""
+    from fiesta_gb300.solver import Solver
+    s = Solver(make_cfg(n, MODES["plain"], dt))
+    s.set_state(U)
+    s.rk_step(nsteps)
+    out = s.get_state()
+    s.close()
     return out
 
 
@@ -708,16 +736,24 @@ def main():
     for m in modes:
         finals[m], results[m] = run_gpu_mode(m, n, a.steps, a.warmup, U0, dt, peak, peak_kind,
                                              a.e2e_steps)
+    if "plain" in finals and len(modes) > 1:
+        finals["plain_perturbed"] = plain_final(n, perturbed(U0), dt, a.warmup + a.steps)
     accuracy = accuracy_report(make_cfg(n, 0, dt), U0, finals, a.warmup + a.steps)
     del finals
     # headline: the fastest mode whose conserved fields stay within rel-L2
     # 1e-5 of the FP64 path (bit-identical to the reference's arithmetic)
+    # headline: the fastest mode whose every state field (conserved and
+    # C-equation) is within max(1e-5, COND_FACTOR x the field's condition
+    # spread) of the FP64 path, which is bit-identical to the reference's
+    # arithmetic
+    spread = (accuracy or {}).get("plain_perturbed_vs_plain", {})
+
     def within(m):
         if m == "plain":
             return True
         rows = (accuracy or {}).get(f"{m}_vs_plain", {})
-        keys = [k for k in rows if not k.startswith(("C", "C_"))]
-        return bool(rows) and max(rows[k] for k in keys) <= 1e-5
+        return bool(rows) and all(e <= max(1e-5, COND_FACTOR * spread.get(k, 0.0))
+                                  for k, e in rows.items())
     ok = [m for m in modes if within(m)] or modes
     head = max(ok, key=lambda m: results[m]["value"])
     # replicas only: each rank runs the whole case; whole-job value sums ranks
@@ -755,8 +791,11 @@ def main():
         "dtype": "f64" if head == "plain" else "f32+f64",
         "data": "synthetic (seeded compiled IC generator: 8 Gaussian pressure kernels, 5 species)",
         "config": {"workload": workload(n), "grid": [n] * 3, "species": 5, "nvt": 14,
-                   "mode": head, "headline_rule": "fastest mode with every conserved field "
-                   "within rel-L2 1e-5 of the FP64 path after warmup+steps steps",
+                   "mode": head, "headline_rule": "fastest mode with every state field "
+                   "(conserved and C-equation) within rel-L2 max(1e-5, 10 x its condition "
+                   "spread) of the FP64 path after warmup+steps steps; the condition spread is "
+                   "the FP64 path's own change from a 1e-9 relative perturbation of the "
+                   "initial state (accuracy.plain_perturbed_vs_plain)",
                    "dt": dt, "l2": f"state {(n + 6) ** 3 * 14 * 8 / 1e9:.2f} GB "
                    f"{'>' if (n + 6) ** 3 * 14 * 8 > 129e6 else '<'} L2 (129 MB)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
