@@ -63,3 +63,31 @@ def test_expansion_256_two_steps():
     c = np.sqrt((1 + gm1) * p / rho)
     cfg.dt = 0.5 * cfg.dx / float(c.max())
     _check(cfg, U0, 2)
+
+
+def test_expansion_256_twenty_steps():
+    """The two-species expansion at 256^3 for 20 of its 100 steps, bit for
+    bit (the oracle needs ~2 s per step at this size on the GPU host; every
+    step of the plain path is the reference's arithmetic, so the remaining
+    steps repeat what these check)."""
+    sp = [dict(gamma=1.4, M=0.02896, mu=1.8e-5), dict(gamma=1.67, M=0.004, mu=1.8e-5)]
+    cfg = abi.make_config(3, (256, 256, 256), dt=1.0, species=sp, visc=True, ceq=True,
+                          kap=10.0, eps=0.4, alpha=40.0)
+    U0 = initial_conditions(cfg, abi.IC_EXPANSION_3D, 20261204, p_ambient=1e5,
+                            T_ambient=300.0, p_high=1e7, radius=0.1, noise=0.01)
+    import bench
+    cfg.dt = 0.5 * cfg.dx / bench.max_wave_speed(cfg, U0)
+    _check(cfg, U0, 20)
+
+
+def test_mixing_384_mixed_step_vs_oracle():
+    """The five-species mixing case at 384^3 (59 M cells, 390^3 x 14 state
+    values): one mixed-precision step against the FP64 oracle, every field
+    under the bar of tests/accuracy.py, finite, species masses conserved to
+    the fluxes' accuracy."""
+    from tests.accuracy import check_fields, run_pair
+    from tests.test_gpu_mixed import bench_case
+    cfg, U0 = bench_case(384)
+    U, Ur, Up = run_pair(cfg, U0, 1)
+    assert np.isfinite(U).all()
+    check_fields(cfg, U, Ur, Up, U0)

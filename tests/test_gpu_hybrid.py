@@ -87,3 +87,31 @@ def test_hybrid_ablation_and_audit():
                         interior(cfg, Uw[..., v]) - interior(cfg, U0[..., v]))
             assert eh < 0.5 * el, (v, eh, el)
         assert eh < 0.2, (v, eh)
+
+
+@pytest.mark.parametrize("n,steps", [(None, 10), (128, 10)])
+def test_shipped_classifier_holds_the_bar(n, steps):
+    """The classifier shipped in fiesta_gb300/classifier_params.json, at the
+    benchmark's operating point (classification every 4 steps, full-WENO
+    audit every 20), on the five-species mixing case: every state field
+    within the bar of tests/accuracy.py against the FP64 oracle, at 48x40x32
+    with a small step and at 128^3 with the benchmark's time step."""
+    from fiesta_gb300.train_classifier import load_params
+    from tests.accuracy import check_fields, run_pair
+    from tests.test_gpu_mixed import SP5, bench_case
+    got = load_params()
+    assert got is not None, "fiesta_gb300/classifier_params.json is missing"
+    params, meta = got
+    if n is None:
+        cfg = abi.make_config(3, (48, 40, 32), dt=2e-7, species=SP5, visc=True, ceq=True,
+                              kap=10.0, eps=0.4, alpha=40.0, mode=abi.MODE_HYBRID)
+        U0 = initial_conditions(cfg, abi.IC_MIXING_3D, 20261206, p_ambient=1e5,
+                                T_ambient=300.0, nkernels=8)
+    else:
+        cfg, U0 = bench_case(n, abi.MODE_HYBRID)
+    cfg.audit_every, cfg.classify_every = 20, 4
+
+    def setup(s):
+        H.set_params(s, params, meta["threshold"])
+
+    check_fields(cfg, *run_pair(cfg, U0, steps, setup=setup), U0)
