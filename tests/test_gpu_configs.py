@@ -67,16 +67,20 @@ def test_expansion_256_two_steps():
 
 def test_expansion_256_twenty_steps():
     """The two-species expansion at 256^3 for 20 of its 100 steps, bit for
-    bit (the oracle needs ~2 s per step at this size on the GPU host; every
+    bit (the oracle needs ~2.4 s per step at this size on the GPU host; every
     step of the plain path is the reference's arithmetic, so the remaining
-    steps repeat what these check)."""
+    steps repeat what these check).  The reference has no adaptive time step:
+    with dt at CFL 0.5 of the initial state (fluid at rest) the blast's
+    wave speed doubles within two steps and the reference's own run diverges
+    by step 6; dt = 0.5 dx / (2 S0) keeps CFL <= 0.5 against the largest
+    wave speed the blast reaches (~2 S0)."""
     sp = [dict(gamma=1.4, M=0.02896, mu=1.8e-5), dict(gamma=1.67, M=0.004, mu=1.8e-5)]
     cfg = abi.make_config(3, (256, 256, 256), dt=1.0, species=sp, visc=True, ceq=True,
                           kap=10.0, eps=0.4, alpha=40.0)
     U0 = initial_conditions(cfg, abi.IC_EXPANSION_3D, 20261204, p_ambient=1e5,
                             T_ambient=300.0, p_high=1e7, radius=0.1, noise=0.01)
     import bench
-    cfg.dt = 0.5 * cfg.dx / bench.max_wave_speed(cfg, U0)
+    cfg.dt = 0.5 * cfg.dx / (2.0 * bench.max_wave_speed(cfg, U0))
     _check(cfg, U0, 20)
 
 
