@@ -167,19 +167,30 @@ def algorithmic_bytes(kernel, cfg):
         "flux3d": 8 * faces * (nv + 4 + 3 * nv),
         "faces3d": 8 * faces * (3 + ns + 1 + 4 + 18 + 27),
         "cell3d": 8 * inner * (3 * nv + 6 + 18 + 27 + 5 + 2 * nvt),
-        # mixed: FP64 state in, FP32 primitives (+ FP64 p, rho) out
-        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + visc + (6 if ceq else 0)) + 8
+        # mixed, the full primitive pass (all cells): FP64 state in; FP32 Q,
+        # rho, velocity, the pressure pair, [mu], [e, C, the five pair low
+        # parts] out, [FP64 rho]
+        "mprim3d": allc * (8 * nvt + 4 * (nv + 1 + 3 + 2 + visc + (11 if ceq else 0))
                            + 8 * buoy),
-        # cell terms: p, u, v, w, [rho, e, C0..4], [rho64]; old and new
-        # state of the momenta, energy and C-variables
-        "mcell3d": inner * (8 + 12 + (28 if ceq else 0) + 8 * buoy
-                            + 16 * (4 + (5 if ceq else 0))),
+        # cell terms of the momenta and energy: the pressure pair, u, v,
+        # [FP64 rho]; old and new momenta and energy
+        "mcell3d": inner * (8 + 8 + 8 * buoy + 16 * 4),
+        # C-equation: u, v, w, rho, e, the five pair low parts, C0..4; old and
+        # new C variables; the next stage's FP32 C variables (fused stages)
+        "mceq3d": inner * (4 * (3 + 2 + 5 + 5) + 16 * 5 + 4 * 5) if ceq else 0,
         # species: Q_s, u, v, w; old and new state of the species
         "mspec3d": inner * (4 * (ns + 3) + 16 * ns),
         # momenta + energy faces: Q0..3, u, v, w, [mu], [rho, C1..4]; the
         # momenta and energy of U_new read and written
         "mmom3d": inner * (4 * (4 + 3 + visc + (5 if ceq else 0)) + 16 * 4),
     }
+    # fused stages: the species kernel also reads the momenta and energy of
+    # U_new and writes the next stage's primitives of the interior; the
+    # ghost-shell pass covers the remaining cells
+    prim_out = 4 * (nv + 1 + 3 + 2 + visc + (6 if ceq else 0)) + 8 * buoy
+    tab["mspec3d_eos"] = tab["mspec3d"] + inner * (8 * 4 + prim_out)
+    tab["mprim3d_shell"] = (allc - inner) * (8 * nvt + 4 * (nv + 1 + 3 + 2 + visc
+                                                            + (11 if ceq else 0)) + 8 * buoy)
     # generalized grids (plain FP64): primitives read the 9 metrics and write
     # rho, p and the contravariant velocity; the cell pass reads the fluxes,
     # p and the 9 metrics once each
@@ -191,6 +202,7 @@ def algorithmic_bytes(kernel, cfg):
         tab["gen_cell"] = inner * (4 * (2 + 18) + 16 * (4 + (nvt - nv)))
         tab["gen_tvel"] = allc * 4 * (3 + 9 + 3)
     tab["mspec3d_hybrid"] = tab["mspec3d"] + inner * 3
+    tab["mspec3d_hybrid_eos"] = tab["mspec3d_eos"] + inner * 3
     tab["mmom3d_hybrid"] = tab["mmom3d"] + inner * 3
     return tab.get(kernel)
 
@@ -274,16 +286,22 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
         per_ms = tot / nl
         b = algorithmic_bytes(name, cfg)
         ach = b / (per_ms / 1e3) / 1e9 if b else None
+        tr = read_traffic(name)
         roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak_gbs, "unit": "GB/s",
-                "frac": ach / peak_gbs if ach else None, "traffic": read_traffic(name),
+                "frac": ach / peak_gbs if ach else None, "traffic": tr,
+                "traffic_source": ("DRAM read + write bytes of a committed ncu capture of this "
+                                   "kernel on the same case at 128^3, scaled by the cells "
+                                   "(x8); not measured in this run") if tr else None,
                 "algorithmic_bytes_per_launch": b, "avg_launch_ms": per_ms,
                 "peak_source": peak_kind,
                 "share_of_step": tot / ms}
         if mode_name == "plain":  # the FP64 pipe, not HBM, is this kernel's roof
+            from fiesta_gb300.solver import fp64_rate
+            roof["fp64_peak_gflops_measured"] = fp64_rate(stream.cuda_stream)
             roof["bound"] = "fp64"
-            roof["bound_note"] = ("FP64 pipe 85 % busy, DRAM a few % (ncu, "
-                                  "profiles/flux3d_plain_64cubed.md); the GB/s figures show how "
-                                  "far below the HBM roof an FP64-bound kernel sits")
+            roof["bound_note"] = ("FP64 pipe 85 % busy, DRAM a few % (an ncu capture of "
+                                  "k_flux3d at 64^3); the GB/s figures show how far below the "
+                                  "HBM roof an FP64-bound kernel sits")
 
     # end to end through the C ABI with host buffers: upload, step, download.
     # One untimed round trip first; then every step is bracketed by events

@@ -233,6 +233,22 @@ size_t work_doubles_per_cell(const fst_config& cf, const Geo& g) {
   return w;
 }
 
+// FP64 FMA throughput: 8 independent FMA chains per thread, every SM full.
+__global__ void __launch_bounds__(256) k_fp64_rate(double* __restrict__ out, int iters) {
+  double a[8];
+  const double x = 1.0 + 1e-9 * threadIdx.x, y = 1.0 - 1e-9 * blockIdx.x;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) a[q] = q;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = fma(a[q], x, y);
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) sum += a[q];
+  if (sum == 12345.678) out[0] = sum;  // keeps the chains live
+}
+
 __global__ void k_nonfinite(const double* __restrict__ U, long long n, int* flag) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   for (; t < n; t += (long long)gridDim.x * blockDim.x)
@@ -764,6 +780,30 @@ int fst_noise_filter(fst_ctx* c, const fst_noise_params* np) {
       fst_noise_launch(g, c->cf, c->Ua, c->dnoise, c->dnoise_key, *np, c->stream, &c->prof,
                        &c->noise_graph);
   return check_launch(c, "noise filter");
+}
+
+int fst_fp64_rate(void* cuda_stream, double* gflops) {
+  if (!gflops) return FST_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, iters = 4096;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return FST_ERR_CUDA;
+  k_fp64_rate<<<blocks, 256, 0, st>>>(nullptr, 64);  // warm-up
+  cudaEventRecord(e0, st);
+  k_fp64_rate<<<blocks, 256, 0, st>>>(nullptr, iters);
+  cudaEventRecord(e1, st);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess || ms <= 0.f) return FST_ERR_CUDA;
+  *gflops = 2.0 * 8.0 * iters * (double)blocks * 256.0 / (ms * 1e-3) / 1e9;
+  return FST_OK;
 }
 
 int fst_check_finite(fst_ctx* c) {

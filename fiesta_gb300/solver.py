@@ -44,6 +44,7 @@ _EXPORTS = {
     "fst_rk_step": (C.c_int, [C.c_void_p, C.c_int]),
     "fst_secondary": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_check_finite": (C.c_int, [C.c_void_p]),
+    "fst_fp64_rate": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "fst_noise_filter": (C.c_int, [C.c_void_p, C.POINTER(abi.FstNoiseParams)]),
     "fst_grid_size": (C.c_size_t, [C.POINTER(abi.FstConfig)]),
     "fst_metrics_size": (C.c_size_t, [C.POINTER(abi.FstConfig)]),
@@ -84,6 +85,15 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def fp64_rate(stream=None):
+    """FP64 FMA throughput of the current device in GFLOP/s (fst_fp64_rate)."""
+    out = C.c_double()
+    rc = lib().fst_fp64_rate(C.c_void_p(stream) if stream else None, C.byref(out))
+    if rc != 0:
+        raise FstError(rc, "fst_fp64_rate failed")
+    return out.value
 
 
 class FstError(RuntimeError):

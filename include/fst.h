@@ -195,6 +195,12 @@ int fst_secondary(fst_ctx* ctx, double* varx, size_t n);
 /* Scan the state for NaN/Inf (sets stats.nonfinite); FST_ERR_NONFINITE if any. */
 int fst_check_finite(fst_ctx* ctx);
 
+/* FP64 fused multiply-add throughput of the current device, in GFLOP/s
+ * (2 per FMA), timed on `cuda_stream` with a kernel of independent FMA
+ * chains over every SM.  No counterpart in the reference: it is the FP64
+ * roof against which the plain FP64 path's kernels are judged. */
+int fst_fp64_rate(void* cuda_stream, double* gflops);
+
 /* Interior minimum and maximum of every state variable (vmin/vmax: nvt
  * values) and, when xmin/xmax are given, of the secondary variables of
  * fst_secondary recomputed from the current state (ndim+3 values: velocity,
