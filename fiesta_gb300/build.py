@@ -76,7 +76,7 @@ def build(force=False, verbose=False, ptxas_v=False):
         objs.append(obj)
     for f in HOST_UNITS:
         obj = os.path.join(BUILD, f + ".o")
-        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c",
+        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", *inc, "-c",
                      os.path.join(CSRC, f), "-o", obj])
         objs.append(obj)
 
@@ -92,7 +92,7 @@ def build(force=False, verbose=False, ptxas_v=False):
         if r.returncode != 0:
             raise RuntimeError("compile failed: " + " ".join(cmd))
     tmp = LIB + ".tmp"
-    link = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    link = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

@@ -111,3 +111,39 @@ __device__ __forceinline__ bool fst_finite(double x) {
 __device__ __forceinline__ long long fst_idx(const Geo& g, int i, int j, int k) {
   return (long long)i + g.sy * j + g.sz * k;
 }
+
+// The ghost cells of a grid in a flat order: the ghost planes in k (3D), the
+// ghost rows in j of the interior planes, the ghost columns in i of the
+// interior rows (each part contiguous along i).  fst_shell_count gives their
+// number; fst_shell_cell maps t in [0, count) to (i, j, k).
+__host__ __device__ __forceinline__ long long fst_shell_count(const Geo& g) {
+  const int ngz = g.ndim == 3 ? g.ng : 0;
+  const long long nk = g.ngk - 2 * ngz, nj = g.ngj - 2 * g.ng;
+  return 2LL * ngz * g.ngi * g.ngj + nk * 2 * g.ng * g.ngi + nk * nj * 2 * g.ng;
+}
+__device__ __forceinline__ void fst_shell_cell(const Geo& g, long long t, int& i, int& j,
+                                               int& k) {
+  const int ng = g.ng, ngz = g.ndim == 3 ? g.ng : 0;
+  const int nj = g.ngj - 2 * ng, nk = g.ngk - 2 * ngz;
+  const long long pl = (long long)g.ngi * g.ngj;
+  const long long nA = 2LL * ngz * pl, nB = (long long)nk * 2 * ng * g.ngi;
+  if (t < nA) {
+    const long long p = t / pl, r = t - p * pl;
+    k = p < ngz ? (int)p : g.ngk - 2 * ngz + (int)p;
+    j = (int)(r / g.ngi);
+    i = (int)(r - (long long)j * g.ngi);
+  } else if (t < nA + nB) {
+    const long long u = t - nA, row = u / g.ngi;
+    i = (int)(u - row * g.ngi);
+    const int kk = (int)(row / (2 * ng)), jj = (int)(row - (long long)kk * 2 * ng);
+    k = ngz + kk;
+    j = jj < ng ? jj : g.ngj - 2 * ng + jj;
+  } else {
+    const long long u = t - nA - nB, row = u / (2 * ng);
+    const int ii = (int)(u - row * 2 * ng);
+    const int kk = (int)(row / nj), jj = (int)(row - (long long)kk * nj);
+    k = ngz + kk;
+    j = ng + jj;
+    i = ii < ng ? ii : g.ngi - 2 * ng + ii;
+  }
+}

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "../../include/fst.h"
@@ -110,6 +111,26 @@ double mix_R(const fst_config* c, const double* Y, int ns) {
   double r = 0.0;
   for (int s = 0; s < ns; ++s) r = r + Y[s] * (c->R / c->M[s]);
   return r;
+}
+
+// Run f(kb, ke) over [k0, k1) split into contiguous plane ranges, one per
+// hardware thread (a few planes or a small grid: the calling thread alone).
+template <class F>
+void parallel_planes(int k0, int k1, const F& f) {
+  const int n = k1 - k0;
+  int nt = (int)std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  if (nt > n) nt = n;
+  if (nt <= 1 || n < 8) {
+    f(k0, k1);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t) {
+    const int kb = k0 + (int)((long long)n * t / nt), ke = k0 + (int)((long long)n * (t + 1) / nt);
+    th.emplace_back([&f, kb, ke] { f(kb, ke); });
+  }
+  for (auto& x : th) x.join();
 }
 
 }  // namespace
@@ -233,8 +254,11 @@ int fst_fill_initial_conditions(const fst_config* c, const fst_ic_params* ic, do
         ba[s] = rng.uniform(0.5, 1.0);
         bw[s] = rng.uniform(0.05, 0.15) * L;
       }
-      double Y[FST_MAX_SPECIES];
-      for (int k = k0; k < k1; ++k)
+      // planes in parallel: every cell's value depends on its position and the
+      // draws above only, so the bits do not depend on the thread count
+      auto planes = [&](int kb, int ke) {
+        double Y[FST_MAX_SPECIES], rho_s[FST_MAX_SPECIES], u[3] = {0, 0, 0};
+        for (int k = kb; k < ke; ++k)
         for (int j = g.ng; j < g.ng + g.ncj; ++j)
           for (int i = g.ng; i < g.ng + g.nci; ++i) {
             double x = cx(i), y = cy(j), z = g.ndim == 3 ? cz(k) : 0.0;
@@ -263,6 +287,8 @@ int fst_fill_initial_conditions(const fst_config* c, const fst_ic_params* ic, do
             for (int s = 0; s < ns; ++s) rho_s[s] = Y[s] * rho;
             put_cell(c, g, U, i, j, k, rho_s, u, p);
           }
+      };
+      parallel_planes(k0, k1, planes);
       break;
     }
     case FST_IC_RT_2D: {

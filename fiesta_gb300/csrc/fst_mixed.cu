@@ -79,41 +79,16 @@ __global__ void __launch_bounds__(256) k_mprim3(Geo g, Geo gq, Phys P,
   }
 }
 
-// The ghost cells of the 3D primitive pass: the 2*ng ghost planes in k, the
-// ghost rows in j of the interior planes, the ghost columns in i of the
-// interior rows, one thread per cell.  Fused stages compute the interior in
-// the previous stage's last kernel and only these after the boundary fill.
+// The ghost cells of the 3D primitive pass (fst_shell_cell order), one
+// thread per cell.  Fused stages compute the interior in the previous
+// stage's last kernel and only these after the boundary fill.
 template <int NS>
 __global__ void __launch_bounds__(256) k_mprim3_shell(Geo g, Geo gq, Phys P,
                                                       const double* __restrict__ U, Prim3Out O) {
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
-  const int ng = g.ng, nk = g.ngk - 2 * ng, nj = g.ngj - 2 * ng;
-  const long long pl = (long long)g.ngi * g.ngj;
-  const long long nA = 2LL * ng * pl;                   // ghost planes
-  const long long nB = (long long)nk * 2 * ng * g.ngi;  // ghost rows of interior planes
-  const long long nC = (long long)nk * nj * 2 * ng;     // ghost columns of interior rows
+  if (t >= fst_shell_count(g)) return;
   int i, j, k;
-  if (t < nA) {
-    const long long p = t / pl, r = t - p * pl;
-    k = p < ng ? (int)p : g.ngk - 2 * ng + (int)p;
-    j = (int)(r / g.ngi);
-    i = (int)(r - (long long)j * g.ngi);
-  } else if (t < nA + nB) {
-    const long long u = t - nA, row = u / g.ngi;
-    i = (int)(u - row * g.ngi);
-    const int kk = (int)(row / (2 * ng)), jj = (int)(row - (long long)kk * 2 * ng);
-    k = ng + kk;
-    j = jj < ng ? jj : g.ngj - 2 * ng + jj;
-  } else if (t < nA + nB + nC) {
-    const long long u = t - nA - nB, row = u / (2 * ng);
-    const int ii = (int)(u - row * 2 * ng);
-    const int kk = (int)(row / nj), jj = (int)(row - (long long)kk * nj);
-    k = ng + kk;
-    j = ng + jj;
-    i = ii < ng ? ii : g.ngi - 2 * ng + ii;
-  } else {
-    return;
-  }
+  fst_shell_cell(g, t, i, j, k);
   float lS = 0.f, lC = 0.f;
   mprim3_cell<NS>(g, gq, P, U, O, false, i, j, k, lS, lC);
 }
@@ -129,21 +104,17 @@ __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
 }
 
 // ghost cells of the stage-1 buffer: U1 = U + (0.5*dt)*0 (src/rk.cpp:42-50).
-// One 64-thread block per (j, k) row: a row with ghost j or k is copied
-// whole, an interior row only its 2*ng ghost cells in i.
-__global__ void __launch_bounds__(64) k_mghost(Geo g, const double* __restrict__ Uold,
-                                               double* __restrict__ Unew) {
-  const int j = blockIdx.x, k = blockIdx.y;
-  const bool row_in = j >= g.ng && j < g.ngj - g.ng &&
-                      (g.ndim == 2 || (k >= g.ng && k < g.ngk - g.ng));
-  const long long c0 = g.sy * j + g.sz * k;
-  const int n = row_in ? 2 * g.ng : g.ngi;
-  for (int t = threadIdx.x; t < n * g.nvt; t += 64) {
-    const int v = t / n, q = t - v * n;
-    const int i = row_in ? (q < g.ng ? q : g.ngi - 2 * g.ng + q) : q;
-    const long long c = c0 + i + g.sv * v;
-    Unew[c] = Uold[c];
-  }
+// One thread per (ghost cell, variable), the cells in fst_shell_cell order.
+__global__ void __launch_bounds__(256) k_mghost(Geo g, long long nshell,
+                                                const double* __restrict__ Uold,
+                                                double* __restrict__ Unew) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= nshell * g.nvt) return;
+  const int v = (int)(t / nshell);
+  int i, j, k;
+  fst_shell_cell(g, t - (long long)v * nshell, i, j, k);
+  const long long c = (long long)i + g.sy * j + g.sz * k + g.sv * v;
+  Unew[c] = Uold[c];
 }
 
 inline unsigned cdiv(long long a, int b) { return (unsigned)((a + b - 1) / b); }
@@ -171,9 +142,7 @@ void launch_mprim3(const Geo& g, const Phys& P, const MixedBufs& b, const double
                    bool shell = false) {
   const Prim3Out O = prim3_out(P, b, all_outputs);
   if (shell) {
-    const long long nk = g.ngk - 2 * g.ng, nj = g.ngj - 2 * g.ng;
-    const long long n = 2LL * g.ng * g.ngi * g.ngj + nk * 2 * g.ng * g.ngi + nk * nj * 2 * g.ng;
-    const unsigned nb = cdiv(n, 256);
+    const unsigned nb = cdiv(fst_shell_count(g), 256);
     switch (g.ns) {
       case 1: k_mprim3_shell<1><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
       case 2: k_mprim3_shell<2><<<nb, 256, 0, st>>>(g, b.gq, P, U, O); break;
@@ -382,7 +351,8 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
                dispatch_rhs<false>(g, P, M, b.red, nullptr, Uold, Unew, coef, Rout, st));
   if (ghosts && !Rout)
     FST_LAUNCH(prof, "mghost", st, n,
-               k_mghost<<<dim3(g.ngj, g.ngk), 64, 0, st>>>(g, Uold, Unew));
+               k_mghost<<<cdiv(fst_shell_count(g) * g.nvt, 256), 256, 0, st>>>(
+                   g, fst_shell_count(g), Uold, Unew));
   if (fuse) {  // the next stage reads what this one wrote into the other set
     fst_mixed_swap(b);
     b.fused_for = Unew;
