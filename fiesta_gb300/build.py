@@ -101,6 +101,75 @@ def build(force=False, verbose=False, ptxas_v=False):
     return LIB
 
 
+DECK_LIB = os.path.join(HERE, "libfst_deck.so")
+LUA_UNITS = ["lapi", "lcode", "lctype", "ldebug", "ldo", "ldump", "lfunc", "lgc", "llex", "lmem",
+             "lobject", "lopcodes", "lparser", "lstate", "lstring", "ltable", "ltm", "lundump",
+             "lvm", "lzio", "lauxlib", "lbaselib", "lbitlib", "lcorolib", "ldblib", "liolib",
+             "lmathlib", "loslib", "lstrlib", "ltablib", "lutf8lib", "loadlib", "linit"]
+
+
+def lua_sources():
+    """The Lua 5.3 sources to build the deck reader against: FST_LUA_SRC,
+    tpls/lua/src of the FIESTA tree named by FST_REFERENCE (by default
+    /root/reference), or the copy staged in oracle/_ref/lua.  None when none
+    exists."""
+    cands = [os.environ.get("FST_LUA_SRC"),
+             os.path.join(os.environ.get("FST_REFERENCE", "/root/reference"), "tpls", "lua", "src"),
+             # the copy the reference checker's recipe (oracle/ref_build.sh) stages for
+             # hosts without the tree, where the tests use it
+             os.path.join(HERE, "..", "oracle", "_ref", "lua")]
+    for c in cands:
+        if c and os.path.exists(os.path.join(c, "lua.h")):
+            return c
+    return None
+
+
+def build_deck(force=False, verbose=False):
+    """Compile fiesta_gb300/libfst_deck.so: the Lua deck reader
+    (csrc/fst_deck.cpp, include/fst_deck.h) and the Lua 5.3 library from the
+    sources lua_sources() finds (compiled where they lie, as the reference's
+    tpls/lua/CMakeLists.txt builds them: LUA_USE_LINUX).  Returns the path,
+    or None when no Lua sources are present (the library is then absent)."""
+    src = lua_sources()
+    if src is None:
+        return None
+    dsrc = os.path.join(CSRC, "fst_deck.cpp")
+    deps = [dsrc, os.path.join(HERE, "..", "include", "fst_deck.h"),
+            os.path.join(HERE, "..", "include", "fst.h")]
+    if (not force and os.path.exists(DECK_LIB)
+            and all(os.path.getmtime(x) <= os.path.getmtime(DECK_LIB) for x in deps)):
+        return DECK_LIB
+    bdir = os.path.join(BUILD, "lua")
+    os.makedirs(bdir, exist_ok=True)
+    cmds, objs = [], []
+    for u in LUA_UNITS:
+        obj = os.path.join(bdir, u + ".o")
+        cmds.append(["gcc", "-O2", "-std=gnu99", "-fPIC", "-DLUA_USE_LINUX", "-w", "-c",
+                     os.path.join(src, u + ".c"), "-o", obj])
+        objs.append(obj)
+    obj = os.path.join(BUILD, "fst_deck.o")
+    cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-I", src, "-c", dsrc, "-o", obj])
+    objs.append(obj)
+
+    def run(cmd):
+        return cmd, subprocess.run(cmd, capture_output=True, text=True)
+
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        for cmd, r in ex.map(run, cmds):
+            if verbose or r.returncode != 0:
+                sys.stderr.write(r.stdout + r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError("compile failed: " + " ".join(cmd))
+    tmp = DECK_LIB + ".tmp"
+    r = subprocess.run(["g++", "-shared", "-o", tmp, *objs, "-ldl", "-lm"], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("link failed")
+    os.replace(tmp, DECK_LIB)
+    return DECK_LIB
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True, ptxas_v="--ptxas" in sys.argv)
     print(LIB)

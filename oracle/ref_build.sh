@@ -8,8 +8,9 @@
 # The reference tree is read where it lies (FST_REFERENCE, default
 # /root/reference).  A machine without it (the GPU host) builds the same
 # library from the bundle this recipe leaves in oracle/_ref/ where the tree
-# is present: the reference files these units include, and the sample decks,
-# copied into oracle/_ref/src and oracle/_ref/samples.  oracle/_ref/ is
+# is present: the reference files these units include, the sample decks and
+# the vendored Lua 5.3 sources, copied into oracle/_ref/src, oracle/_ref/samples
+# and oracle/_ref/lua.  oracle/_ref/ is
 # git-ignored: the bundle travels with the working tree and is never
 # committed.  Reference files compiled:
 #   src/cart3d.cpp src/cart2d.cpp src/rk.cpp src/rkfunction.cpp  (-DHAVE_MPI:
@@ -51,6 +52,12 @@ if [ "$STAGE" = 1 ]; then
   for f in $(echo "$deps" | tr ' \\' '\n\n' | grep "^$REF/src/" | sort -u); do
     cp "$f" "$OUT/src/"
   done
+  # the Lua 5.3 sources the reference vendors, for the Lua deck reader's
+  # tests on a host without the tree (fiesta_gb300/build.py build_deck)
+  if [ -d "$REF/tpls/lua/src" ]; then
+    mkdir -p "$OUT/lua"
+    cp "$REF"/tpls/lua/src/*.c "$REF"/tpls/lua/src/*.h "$OUT/lua/"
+  fi
   for d in "$REF"/samples/*/; do
     if [ -f "$d/fiesta.lua" ]; then
       mkdir -p "$OUT/samples/$(basename "$d")"
