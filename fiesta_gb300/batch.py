@@ -12,7 +12,10 @@ from .solver import FstError, initial_conditions, lib
 class BatchInfo(C.Structure):
     _fields_ = [("ncases", C.c_int), ("tile_height", C.c_int), ("tiles", C.c_int),
                 ("persistent_blocks", C.c_int), ("launches_per_step", C.c_int),
-                ("reserved", C.c_int), ("interior_cells", C.c_int64)]
+                ("tile_width", C.c_int), ("interior_cells", C.c_int64),
+                ("blocks_per_sm", C.c_int), ("max_blocks_per_sm", C.c_int),
+                ("tune_candidates", C.c_int), ("reserved", C.c_int),
+                ("tune_best_ms", C.c_double), ("tune_worst_ms", C.c_double)]
 
 
 _SIGS = {
@@ -25,6 +28,7 @@ _SIGS = {
     "fst_batch_synchronize": (C.c_int, [C.c_void_p]),
     "fst_batch_stream": (C.c_void_p, [C.c_void_p]),
     "fst_batch_set_tile_height": (C.c_int, [C.c_void_p, C.c_int]),
+    "fst_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "fst_batch_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
     "fst_batch_tune": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
 }
@@ -89,10 +93,19 @@ class Batch:
     def set_tile_height(self, h):
         self._check(_L().fst_batch_set_tile_height(self._b, int(h)), "set_tile_height")
 
+    def set_tile(self, width, height, blocks_per_sm=0):
+        """RHS tile of width x height threads and persistent blocks per SM
+        (0: the occupancy limit)."""
+        self._check(_L().fst_batch_set_tile(self._b, int(width), int(height), int(blocks_per_sm)),
+                    "set_tile")
+
     def tune(self, json_path=None, force=False):
+        """Pick the fastest tile shape and blocks per SM on this ensemble;
+        returns (width, height, blocks_per_sm)."""
         p = json_path.encode() if json_path else None
         self._check(_L().fst_batch_tune(self._b, p, int(bool(force))), "tune")
-        return self.info()["tile_height"]
+        i = self.info()
+        return i["tile_width"], i["tile_height"], i["blocks_per_sm"]
 
     def info(self):
         i = BatchInfo()

@@ -4,7 +4,7 @@ Translation units and their floating-point contract:
   fst_plain3d.cu, fst_plain2d.cu, fst_bc.cu, fst_noise.cu, fst_gen.cu
                                               --fmad=false: the plain FP64 path
       reproduces the reference's FP64 arithmetic operation for operation
-  fst_mixed.cu, fst_mixed3d.cu, fst_hybrid.cu, fst_batch.cu
+  fst_mixed.cu, fst_mixed3d.cu, fst_hybrid.cu, fst_batch*.cu
                                               FMA on, fast FP32 math
   fst_mixedgen.cu                             IEEE FP32 (pair arithmetic)
   fst_api.cu                                  host orchestration
@@ -34,6 +34,9 @@ UNITS = [
     ("fst_mixed3d.cu", ["--use_fast_math"]),
     ("fst_hybrid.cu", ["--use_fast_math"]),
     ("fst_batch.cu", ["--use_fast_math"]),
+    ("fst_batch_w16.cu", ["--use_fast_math"]),
+    ("fst_batch_w32.cu", ["--use_fast_math"]),
+    ("fst_batch_w64.cu", ["--use_fast_math"]),
     ("fst_api.cu", ["--fmad=false"]),
     ("fst_noalloc.cu", ["--fmad=false"]),
     ("fst_noise.cu", ["--fmad=false"]),
@@ -84,7 +87,7 @@ def build(force=False, verbose=False, ptxas_v=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
 
-    with ThreadPoolExecutor(max_workers=min(8, len(cmds))) as ex:
+    with ThreadPoolExecutor(max_workers=min(max(os.cpu_count() or 1, 4), 16, len(cmds))) as ex:
         results = list(ex.map(run, cmds))
     for cmd, r in results:
         if verbose or r.returncode != 0 or ptxas_v:
@@ -110,11 +113,11 @@ LUA_UNITS = ["lapi", "lcode", "lctype", "ldebug", "ldo", "ldump", "lfunc", "lgc"
 
 def lua_sources():
     """The Lua 5.3 sources to build the deck reader against: FST_LUA_SRC,
-    tpls/lua/src of the FIESTA tree named by FST_REFERENCE (by default
-    /root/reference), or the copy staged in oracle/_ref/lua.  None when none
-    exists."""
+    tpls/lua/src of the FIESTA tree named by FST_REFERENCE (when set), or the
+    copy staged in oracle/_ref/lua.  None when none exists."""
+    ref = os.environ.get("FST_REFERENCE")
     cands = [os.environ.get("FST_LUA_SRC"),
-             os.path.join(os.environ.get("FST_REFERENCE", "/root/reference"), "tpls", "lua", "src"),
+             os.path.join(ref, "tpls", "lua", "src") if ref else None,
              # the copy the reference checker's recipe (oracle/ref_build.sh) stages for
              # hosts without the tree, where the tests use it
              os.path.join(HERE, "..", "oracle", "_ref", "lua")]

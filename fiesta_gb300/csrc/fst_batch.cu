@@ -8,14 +8,17 @@
 //   k_bprim                primitive pass over the concatenated cells of all
 //                          cases (block ranges aligned to cases, so a block's
 //                          per-case maxima reduce to one atomicMax per warp)
-//   k_brhs                 one persistent launch per stage: #SM x occupancy
+//   k_brhs                 one persistent launch per stage: #SM x blocks-per-SM
 //                          blocks walk a global list of (case, tile) work items
 //                          and run the fused 2D RHS + RK tile of fst_mixed
+//                          (fst_batch_dev.cuh; instantiated per tile width in
+//                          fst_batch_w16/w32/w64.cu)
 //   k_bghost               stage-1 ghost copy
 // A whole time step is captured once into a CUDA graph and replayed.  The
-// tile height (threads along j) is picked by an autotuner that times the
-// candidates on the actual ensemble and persists the choice to a JSON file
-// keyed by GPU and ensemble signature.
+// RHS tile shape (width x height threads) and the persistent blocks per SM
+// are picked by an autotuner that times every candidate on the actual
+// ensemble and persists the choice, with the timing of every candidate, to
+// a JSON file keyed by GPU and ensemble signature.
 //
 // The per-cell and per-tile arithmetic is the single-case mixed path's
 // (fst_mixed_dev.cuh), so a batched case evolves exactly like the same case
@@ -28,36 +31,30 @@
 #include <string>
 #include <vector>
 
+#include "fst_batch_dev.cuh"
 #include "fst_bc_dev.cuh"
-#include "fst_mixed_dev.cuh"
 
 using namespace fstm;
+using fstb::BCase;
+using fstb::find_case;
 
 namespace {
 
-struct BCase {
-  Geo g;
-  MixedView M;
-  double *Ua, *Ub;
-  unsigned long long* red;  // 2 keys
-  float* Q;                 // writable views of the mixed buffers
-  float *rho32, *vel32, *T32, *nrg, *C, *lo;
-  double *p64, *rho64;
-  int bc[4];     // xmin, xmax, ymin, ymax
-  int per[2];    // x, y periodic
+// RHS tile shapes (threads along i, along j) the autotuner times: at most
+// 512 threads, so that the NVMAX kernels keep their registers unspilled
+struct TileShape {
+  int w, h;
 };
+constexpr TileShape kShapes[] = {{16, 4}, {16, 8}, {16, 16}, {32, 4}, {32, 8},
+                                 {32, 16}, {64, 4}, {64, 8}};
 
-constexpr int kTileHeights[3] = {4, 8, 16};
-
-__device__ __forceinline__ int find_case(const int* __restrict__ off, int n, int x) {
-  // largest c with off[c] <= x (off has n+1 entries, off[0] = 0)
-  int lo = 0, hi = n;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (off[mid] <= x) lo = mid;
-    else hi = mid;
+const void* brhs_kernel(int w, int h, int nv) {
+  switch (w) {
+    case 16: return fstb::brhs_kernel_w16(h, nv);
+    case 32: return fstb::brhs_kernel_w32(h, nv);
+    case 64: return fstb::brhs_kernel_w64(h, nv);
+    default: return nullptr;
   }
-  return lo;
 }
 
 __global__ void k_binit(const BCase* __restrict__ cs, int n) {
@@ -127,29 +124,6 @@ __global__ void k_bghost(const BCase* __restrict__ cs, const int* __restrict__ b
   for (int v = 0; v < g.nvt; ++v) B.Ub[local + g.sv * v] = B.Ua[local + g.sv * v];
 }
 
-// persistent RHS + RK stage over the (case, tile) work list
-template <int NV, int TYY>
-__global__ void __launch_bounds__(TX * TYY) k_brhs(const BCase* __restrict__ cs,
-                                                   const Phys* __restrict__ Ps,
-                                                   const int* __restrict__ tile_off, int ncase,
-                                                   int stage) {
-  __shared__ float sG[TYY][TX][NV];
-  const int ntile = tile_off[ncase];
-  for (int w = blockIdx.x; w < ntile; w += gridDim.x) {
-    const int c = find_case(tile_off, ncase, w);
-    const BCase& B = cs[c];
-    const Phys& P = Ps[c];
-    const int ntx = (B.g.nci + TX - 2) / (TX - 1);
-    const int local = w - tile_off[c];
-    const double* Uin = stage == 1 ? B.Ua : B.Ub;
-    (void)Uin;
-    // stage 1: Ub = Ua + hdt*R(Ua); stage 2: Ua = Ua + dt*R(Ub)
-    rhs2d_tile<NV, false, TYY>(B.g, P, B.M, B.red, nullptr, B.Ua, stage == 1 ? B.Ub : B.Ua,
-                               stage == 1 ? P.hdt : P.dt, nullptr, local % ntx, local / ntx, sG);
-    __syncthreads();
-  }
-}
-
 inline unsigned cdivu(long long a, int b) { return (unsigned)((a + b - 1) / b); }
 
 }  // namespace
@@ -166,9 +140,14 @@ struct fst_batch {
   int nblocks = 0;
   int ntiles = 0;
   int nv = 0, nvt = 0;
-  int tile_h = 8;
+  int tile_w = 32, tile_h = 8;
+  int bps_req = 0;           // blocks per SM asked for (0: the occupancy limit)
+  int bps = 0, bps_max = 0;  // in use; the occupancy limit of the shape
+  const void* rhs = nullptr;
   int max_lines = 0, max_face = 0;
   int persistent_blocks = 0;
+  int tune_candidates = 0;
+  double tune_best_ms = 0.0, tune_worst_ms = 0.0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaGraph_t graph = nullptr;
@@ -196,45 +175,26 @@ int balloc(fst_batch* b, void** p, size_t bytes) {
   return FST_OK;
 }
 
-// launches of one RK stage; returns launch count
-template <int NV, int TYY>
+// the persistent RHS launch of one RK stage
 int enqueue_rhs(fst_batch* b, int stage) {
-  k_brhs<NV, TYY><<<b->persistent_blocks, dim3(TX, TYY, 1), 0, b->stream>>>(
-      b->dcases, b->dphys, b->dtile_off, (int)b->hcases.size(), stage);
+  int ncase = (int)b->hcases.size();
+  void* args[] = {(void*)&b->dcases, (void*)&b->dphys, (void*)&b->dtile_off, (void*)&ncase,
+                  (void*)&stage};
+  cudaLaunchKernel(b->rhs, dim3(b->persistent_blocks), dim3(b->tile_w, b->tile_h, 1), args, 0,
+                   b->stream);
   return 1;
 }
 
-template <int TYY>
-int enqueue_rhs_nv(fst_batch* b, int stage) {
-  switch (b->nv) {
-    case 4: return enqueue_rhs<4, TYY>(b, stage);
-    case 5: return enqueue_rhs<5, TYY>(b, stage);
-    case 6: return enqueue_rhs<6, TYY>(b, stage);
-    case 7: return enqueue_rhs<7, TYY>(b, stage);
-    case 8: return enqueue_rhs<8, TYY>(b, stage);
-    default: return enqueue_rhs<NVMAX, TYY>(b, stage);
-  }
-}
-
-template <int TYY>
-const void* rhs_kernel(int nv) {
-  switch (nv) {
-    case 4: return (const void*)k_brhs<4, TYY>;
-    case 5: return (const void*)k_brhs<5, TYY>;
-    case 6: return (const void*)k_brhs<6, TYY>;
-    case 7: return (const void*)k_brhs<7, TYY>;
-    case 8: return (const void*)k_brhs<8, TYY>;
-    default: return (const void*)k_brhs<NVMAX, TYY>;
-  }
-}
-
-// tile list for the chosen tile height; persistent grid size by occupancy
+// tile list for the chosen tile shape; persistent grid = SMs x blocks per
+// SM (the request, capped at the shape's occupancy limit)
 int setup_tiles(fst_batch* b) {
+  const void* k = brhs_kernel(b->tile_w, b->tile_h, b->nv);
+  if (!k) return bfail(b, FST_ERR_INVALID, "tile shape not instantiated");
   const int n = (int)b->hcases.size();
   std::vector<int> off(n + 1, 0);
   for (int c = 0; c < n; ++c) {
     const Geo& g = b->geos[c];
-    const int ntx = (g.nci + TX - 2) / (TX - 1);
+    const int ntx = (g.nci + b->tile_w - 2) / (b->tile_w - 1);
     const int nty = (g.ncj + b->tile_h - 2) / (b->tile_h - 1);
     off[c + 1] = off[c] + ntx * nty;
   }
@@ -243,13 +203,15 @@ int setup_tiles(fst_batch* b) {
                                   cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
-  const void* k = b->tile_h == 4 ? rhs_kernel<4>(b->nv)
-                  : b->tile_h == 8 ? rhs_kernel<8>(b->nv) : rhs_kernel<16>(b->nv);
   int per_sm = 0, dev = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TX * b->tile_h, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, b->tile_w * b->tile_h, 0);
+  if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, cudaGetErrorString(e));
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  b->persistent_blocks = std::max(1, per_sm) * sms;
+  b->rhs = k;
+  b->bps_max = std::max(1, per_sm);
+  b->bps = b->bps_req > 0 ? std::min(b->bps_req, b->bps_max) : b->bps_max;
+  b->persistent_blocks = b->bps * sms;
   return FST_OK;
 }
 
@@ -279,9 +241,7 @@ int enqueue_step(fst_batch* b) {
     }
     k_bprim<<<b->nblocks, 256, 0, b->stream>>>(b->dcases, b->dphys, b->dblock_off, n, use_a, ceq);
     ++L;
-    if (b->tile_h == 4) L += enqueue_rhs_nv<4>(b, stage);
-    else if (b->tile_h == 8) L += enqueue_rhs_nv<8>(b, stage);
-    else L += enqueue_rhs_nv<16>(b, stage);
+    L += enqueue_rhs(b, stage);
     if (stage == 1) {
       k_bghost<<<b->nblocks, 256, 0, b->stream>>>(b->dcases, b->dblock_off, n);
       ++L;
@@ -307,6 +267,15 @@ int capture(fst_batch* b) {
   if (e != cudaSuccess) return bfail(b, FST_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e));
   b->launches = L;
   return FST_OK;
+}
+
+// value of `"name": <number>` inside one stored entry line; false if absent
+bool entry_number(const std::string& line, const char* name, double* v) {
+  const std::string k = std::string("\"") + name + "\": ";
+  const size_t at = line.find(k);
+  if (at == std::string::npos) return false;
+  *v = std::atof(line.c_str() + at + k.size());
+  return true;
 }
 
 std::string signature(const fst_batch* b) {
@@ -472,11 +441,18 @@ int fst_batch_synchronize(fst_batch* b) {
 
 void* fst_batch_stream(fst_batch* b) { return b ? (void*)b->stream : nullptr; }
 
-int fst_batch_set_tile_height(fst_batch* b, int h) {
-  if (!b || (h != 4 && h != 8 && h != 16)) return FST_ERR_INVALID;
-  b->tile_h = h;
+int fst_batch_set_tile(fst_batch* b, int width, int height, int blocks_per_sm) {
+  if (!b || blocks_per_sm < 0 || !brhs_kernel(width, height, b->nv)) return FST_ERR_INVALID;
+  b->tile_w = width;
+  b->tile_h = height;
+  b->bps_req = blocks_per_sm;
   int rc = setup_tiles(b);
   return rc ? rc : capture(b);
+}
+
+int fst_batch_set_tile_height(fst_batch* b, int h) {
+  if (!b) return FST_ERR_INVALID;
+  return fst_batch_set_tile(b, b->tile_w, h, b->bps_req);
 }
 
 int fst_batch_info(const fst_batch* b, fst_batch_info_t* out) {
@@ -486,9 +462,16 @@ int fst_batch_info(const fst_batch* b, fst_batch_info_t* out) {
   out->tiles = b->ntiles;
   out->persistent_blocks = b->persistent_blocks;
   out->launches_per_step = (int)b->launches;
+  out->tile_width = b->tile_w;
   long long cells = 0;
   for (auto& g : b->geos) cells += (long long)g.nci * g.ncj;
   out->interior_cells = cells;
+  out->blocks_per_sm = b->bps;
+  out->max_blocks_per_sm = b->bps_max;
+  out->tune_candidates = b->tune_candidates;
+  out->reserved = 0;
+  out->tune_best_ms = b->tune_best_ms;
+  out->tune_worst_ms = b->tune_worst_ms;
   return FST_OK;
 }
 
@@ -504,11 +487,38 @@ int fst_batch_tune(fst_batch* b, const char* json_path, int force) {
       text = ss.str();
     }
   }
-  const std::string needle = "\"key\": \"" + key + "\", \"tile_height\": ";
-  const size_t at = text.find(needle);
-  if (!force && at != std::string::npos) {
-    const int h = std::atoi(text.c_str() + at + needle.size());
-    return fst_batch_set_tile_height(b, h);
+  // the store: {"entries": [ one entry per line ]}, entries keyed by
+  // signature; an entry holds the chosen shape, its time, the slowest
+  // candidate's time and every candidate's ms per step ("WxHxK")
+  const std::string needle = "{\"key\": \"" + key + "\", ";
+  std::vector<std::string> lines;
+  std::string mine;
+  {
+    std::istringstream in(text);
+    std::string ln;
+    while (std::getline(in, ln)) {
+      if (ln.find("\"key\": ") == std::string::npos) continue;
+      while (!ln.empty() && (ln.back() == ',' || ln.back() == ' ')) ln.pop_back();
+      if (ln.find(needle) != std::string::npos) mine = ln;
+      else lines.push_back(ln);
+    }
+  }
+  if (!force && !mine.empty()) {
+    double w, h, k, cand = 0, best = 0, worst = 0;
+    if (entry_number(mine, "tile_width", &w) && entry_number(mine, "tile_height", &h) &&
+        entry_number(mine, "blocks_per_sm", &k)) {
+      entry_number(mine, "candidates", &cand);
+      entry_number(mine, "best_ms", &best);
+      entry_number(mine, "worst_ms", &worst);
+      const int rc = fst_batch_set_tile(b, (int)w, (int)h, (int)k);
+      if (rc == FST_OK) {
+        b->tune_candidates = (int)cand;
+        b->tune_best_ms = best;
+        b->tune_worst_ms = worst;
+        return FST_OK;
+      }
+      // a stored shape this build cannot run: time the candidates again
+    }
   }
   // time each candidate on a few steps of this ensemble (state is restored)
   std::vector<std::vector<double>> saved(b->hcases.size());
@@ -520,43 +530,63 @@ int fst_batch_tune(fst_batch* b, const char* json_path, int force) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  double best = 1e300;
-  int best_h = 8;
+  double best = 1e300, worst = 0.0;
+  TileShape best_s = {32, 8};
+  int best_k = 0, ncand = 0;
   std::ostringstream times;
-  for (int h : kTileHeights) {
-    int rc = fst_batch_set_tile_height(b, h);
-    if (rc) return rc;
-    fst_batch_rk_step(b, 1);
-    cudaEventRecord(e0, b->stream);
-    fst_batch_rk_step(b, 3);
-    cudaEventRecord(e1, b->stream);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    times << (times.tellp() > 0 ? ", " : "") << "\"" << h << "\": " << ms / 3.0;
-    if (ms < best) {
-      best = ms;
-      best_h = h;
+  int rc = FST_OK;
+  for (const TileShape& sh : kShapes) {
+    rc = fst_batch_set_tile(b, sh.w, sh.h, 0);
+    if (rc) break;
+    // blocks per SM: the occupancy limit m and about 3/4, 1/2 and 1/4 of it
+    const int m = b->bps_max;
+    std::vector<int> ks = {m, (3 * m + 3) / 4, (m + 1) / 2, (m + 3) / 4};
+    std::sort(ks.begin(), ks.end());
+    ks.erase(std::unique(ks.begin(), ks.end()), ks.end());
+    for (int k : ks) {
+      rc = fst_batch_set_tile(b, sh.w, sh.h, k);
+      if (rc) break;
+      fst_batch_rk_step(b, 1);
+      cudaEventRecord(e0, b->stream);
+      fst_batch_rk_step(b, 3);
+      cudaEventRecord(e1, b->stream);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) {
+        rc = bfail(b, FST_ERR_CUDA, std::string("tune: ") + cudaGetErrorString(e));
+        break;
+      }
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const double per = ms / 3.0;
+      times << (ncand ? ", " : "") << "\"" << sh.w << "x" << sh.h << "x" << k << "\": " << per;
+      ++ncand;
+      worst = std::max(worst, per);
+      if (per < best) {
+        best = per;
+        best_s = sh;
+        best_k = k;
+      }
     }
+    if (rc) break;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  for (size_t c = 0; c < b->hcases.size(); ++c)
-    fst_batch_set_state(b, (int)c, saved[c].data(), saved[c].size());
-  int rc = fst_batch_set_tile_height(b, best_h);
+  for (size_t c = 0; c < b->hcases.size(); ++c) {
+    const int r2 = fst_batch_set_state(b, (int)c, saved[c].data(), saved[c].size());
+    if (!rc) rc = r2;
+  }
   if (rc) return rc;
+  rc = fst_batch_set_tile(b, best_s.w, best_s.h, best_k);
+  if (rc) return rc;
+  b->tune_candidates = ncand;
+  b->tune_best_ms = best;
+  b->tune_worst_ms = worst;
   if (json_path) {
-    // one entry per line inside {"entries": [ ... ]}
-    std::vector<std::string> lines;
-    std::istringstream in(text);
-    std::string ln;
-    while (std::getline(in, ln))
-      if (ln.find("\"key\": ") != std::string::npos && ln.find(needle) == std::string::npos) {
-        while (!ln.empty() && (ln.back() == ',' || ln.back() == ' ')) ln.pop_back();
-        lines.push_back(ln);
-      }
     std::ostringstream entry;
-    entry << "  {" << needle << best_h << ", \"ms_per_step\": {" << times.str() << "}}";
+    entry << "  " << needle << "\"tile_width\": " << best_s.w << ", \"tile_height\": " << best_s.h
+          << ", \"blocks_per_sm\": " << best_k << ", \"candidates\": " << ncand
+          << ", \"best_ms\": " << best << ", \"worst_ms\": " << worst << ", \"ms_per_step\": {"
+          << times.str() << "}}";
     lines.push_back(entry.str());
     std::ofstream f(json_path);
     f << "{\"entries\": [\n";

@@ -1,0 +1,7 @@
+// fst_batch_w32.cu — the persistent batched RHS kernels of tile width 32
+// (every tile height and species count; see fst_batch_dev.cuh).
+#include "fst_batch_dev.cuh"
+
+namespace fstb {
+const void* brhs_kernel_w32(int tyy, int nv) { return brhs_kernel_for<32>(tyy, nv); }
+}  // namespace fstb

@@ -501,18 +501,25 @@ __device__ __forceinline__ void face2d(const Geo& g, const Phys& P, const MixedV
   G[2] -= V[2] * fc.rd[f];
 }
 
-// One 32 x TYY thread tile of the fused 2D RHS + RK stage (tile (bx, by) of
-// the case).  sG is the block's shared staging of the y faces.  All threads
-// of the block must call it (it synchronises).
-template <int NV, bool HYB, int TYY>
+// One TXX x TYY thread tile of the fused 2D RHS + RK stage (tile (bx, by)
+// of the case; TXX = 16, 32 or 64 threads along i).  sG is the block's
+// shared staging of the y faces; the x face left of a cell comes from the
+// neighbouring lane by shuffle (within TXX lanes when TXX < 32), and for
+// TXX = 64 the first lane of the second warp of a row reads it from sE,
+// where the last lane of the first warp left it.  All threads of the block
+// must call it (it synchronises).
+template <int NV, bool HYB, int TYY, int TXX = TX>
 __device__ __forceinline__ void rhs2d_tile(const Geo& g, const Phys& P, const MixedView& M,
                                            const unsigned long long* __restrict__ red,
                                            const unsigned char* __restrict__ smap,
                                            const double* Uold, double* Unew, double coef,
                                            double* __restrict__ Rout, int bx, int by,
-                                           float (*sG)[TX][NV]) {
+                                           float (*sG)[TXX][NV], float (*sE)[NV] = nullptr) {
+  static_assert(TXX == 16 || TXX == 32 || TXX == 64, "tile width 16, 32 or 64");
+  constexpr int kWarpsX = TXX > 32 ? TXX / 32 : 1;
+  constexpr int kShflW = TXX < 32 ? TXX : 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i = g.ng - 1 + bx * (TX - 1) + tx;
+  const int i = g.ng - 1 + bx * (TXX - 1) + tx;
   const int j = g.ng - 1 + by * (TYY - 1) + ty;
   const long long sv = g.sv, sy = g.sy;
   const int nv = P.nv;
@@ -531,11 +538,17 @@ __device__ __forceinline__ void rhs2d_tile(const Geo& g, const Phys& P, const Mi
   if (fj && ci) face2d<NV, HYB>(g, P, M, fc, c, 1, HYB && smooth_at(smap, c, 1), nv, Gy);
 #pragma unroll
   for (int v = 0; v < NV; ++v) sG[ty][tx][v] = Gy[v];
+  if (kWarpsX > 1 && (tx & 31) == 31) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sE[ty * kWarpsX + (tx >> 5)][v] = Gx[v];
+  }
   __syncthreads();
+  const bool edge = kWarpsX > 1 && (tx & 31) == 0 && tx > 0;
   float R[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
-    const float gxl = __shfl_up_sync(0xffffffffu, Gx[v], 1);
+    float gxl = __shfl_up_sync(0xffffffffu, Gx[v], 1, kShflW);
+    if (edge) gxl = sE[ty * kWarpsX + (tx >> 5) - 1][v];
     R[v] = 0.f;
     if (ci && cj) R[v] = -((Gx[v] - gxl) + (Gy[v] - sG[ty - 1][tx][v]));
   }

@@ -315,8 +315,14 @@ typedef struct fst_batch_info_t {
   int tiles;              /* work items per stage                         */
   int persistent_blocks;  /* blocks of the persistent RHS launch          */
   int launches_per_step;  /* kernels in the captured step graph           */
-  int reserved;
+  int tile_width;         /* threads along i of the RHS tile (16, 32, 64) */
   int64_t interior_cells; /* sum over cases                               */
+  int blocks_per_sm;      /* persistent blocks per SM in use              */
+  int max_blocks_per_sm;  /* the occupancy limit of the tile shape        */
+  int tune_candidates;    /* candidates the autotuner timed (0: not tuned) */
+  int reserved;
+  double tune_best_ms;    /* ms per step of the chosen candidate          */
+  double tune_worst_ms;   /* ms per step of the slowest candidate         */
 } fst_batch_info_t;
 int fst_batch_create(const fst_config* cfgs, int ncases, fst_batch** out);
 void fst_batch_destroy(fst_batch* b);
@@ -326,11 +332,19 @@ int fst_batch_get_state(fst_batch* b, int case_index, double* U, size_t n);
 int fst_batch_rk_step(fst_batch* b, int nsteps);
 int fst_batch_synchronize(fst_batch* b);
 void* fst_batch_stream(fst_batch* b);  /* the cudaStream_t the graph runs on */
-int fst_batch_set_tile_height(fst_batch* b, int tile_height);
+/* RHS tile shape: width x height threads, (16|32) x (4|8|16) or 64 x (4|8),
+ * and persistent blocks per SM (0: the occupancy limit of the shape; larger
+ * requests are capped at it).  Recaptures the step graph. */
+int fst_batch_set_tile(fst_batch* b, int width, int height, int blocks_per_sm);
+int fst_batch_set_tile_height(fst_batch* b, int tile_height);  /* keeps width, blocks */
 int fst_batch_info(const fst_batch* b, fst_batch_info_t* out);
-/* Autotuner: time every tile height on this ensemble (state restored
- * afterwards) and keep the fastest; with json_path, reuse a stored choice for
- * the same GPU and ensemble signature unless `force`, and store new ones. */
+/* Autotuner: time every tile shape (width x height above) at up to four
+ * persistent blocks-per-SM counts (the occupancy limit and about 3/4, 1/2
+ * and 1/4 of it) on this ensemble, 3 graph replays each after one warm-up
+ * (state restored afterwards), and keep the fastest.  With json_path, reuse a
+ * stored choice for the same GPU and ensemble signature unless `force`, and
+ * store new ones with every candidate's ms per step.  fst_batch_info reports
+ * the chosen and the slowest candidate's times. */
 int fst_batch_tune(fst_batch* b, const char* json_path, int force);
 
 /* Learned smoothness classifier (FST_MODE_HYBRID).  No counterpart in the

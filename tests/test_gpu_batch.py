@@ -68,13 +68,62 @@ def test_batch_tune_persists_choice(tmp_path):
     for c, U in enumerate(states):
         b.set_state(c, U)
     path = str(tmp_path / "tune.json")
-    h = b.tune(path)
-    assert h in (4, 8, 16)
+    w, h, k = b.tune(path)
+    assert w in (16, 32, 64) and h in (4, 8, 16) and w * h <= 512 and k >= 1
     d = json.load(open(path))
-    assert len(d["entries"]) == 1 and d["entries"][0]["tile_height"] == h
-    assert set(d["entries"][0]["ms_per_step"]) == {"4", "8", "16"}
+    assert len(d["entries"]) == 1
+    e = d["entries"][0]
+    assert (e["tile_width"], e["tile_height"], e["blocks_per_sm"]) == (w, h, k)
+    shapes = {tuple(int(x) for x in key.split("x")[:2]) for key in e["ms_per_step"]}
+    assert shapes == {(16, 4), (16, 8), (16, 16), (32, 4), (32, 8), (32, 16), (64, 4), (64, 8)}
+    assert e["candidates"] == len(e["ms_per_step"]) > len(shapes)
+    assert e["best_ms"] == pytest.approx(min(e["ms_per_step"].values()), rel=1e-4)
+    assert e["worst_ms"] == pytest.approx(max(e["ms_per_step"].values()), rel=1e-4)
+    i = b.info()
+    assert i["tune_candidates"] == e["candidates"] and i["tune_worst_ms"] >= i["tune_best_ms"] > 0
     # the stored choice is reused without timing, and the state was restored
     b2 = Batch(cfgs)
-    assert b2.tune(path) == h
+    assert b2.tune(path) == (w, h, k)
+    assert b2.info()["tune_best_ms"] == pytest.approx(e["best_ms"])
     assert np.array_equal(b.get_state(0), states[0])
     assert b.info()["launches_per_step"] >= 8
+    # another ensemble gets its own entry beside the first
+    b3 = Batch(cfgs[:3])
+    for c in range(3):
+        b3.set_state(c, states[c])
+    b3.tune(path)
+    assert len(json.load(open(path))["entries"]) == 2
+
+
+@pytest.mark.parametrize("shape", [(16, 4), (16, 16), (32, 4), (32, 16), (64, 4), (64, 8)])
+def test_batch_every_tile_shape_matches_the_default(shape):
+    """Every shape the autotuner may pick gives the bits of the 32 x 8 tile
+    (same per-face and per-cell arithmetic, only the work split differs), at
+    one and at the full persistent block count."""
+    cfgs, states = small_ensemble()
+    ref = Batch(cfgs)
+    for c, U in enumerate(states):
+        ref.set_state(c, U)
+    ref.set_tile(32, 8)
+    ref.rk_step(3)
+    for k in (1, 0):
+        b = Batch(cfgs)
+        for c, U in enumerate(states):
+            b.set_state(c, U)
+        b.set_tile(*shape, k)
+        i = b.info()
+        assert (i["tile_width"], i["tile_height"]) == shape
+        assert i["blocks_per_sm"] == (1 if k == 1 else i["max_blocks_per_sm"])
+        b.rk_step(3)
+        for c in range(len(cfgs)):
+            assert np.array_equal(b.get_state(c), ref.get_state(c)), (shape, k, c)
+
+
+def test_batch_rejects_shapes_it_has_no_kernel_for():
+    cfgs, states = small_ensemble()
+    b = Batch(cfgs)
+    for bad in [(64, 16), (8, 8), (32, 2), (128, 4)]:
+        with pytest.raises(Exception):
+            b.set_tile(*bad)
+    with pytest.raises(Exception):
+        b.set_tile(32, 8, -1)
