@@ -304,13 +304,19 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
                                   "HBM roof an FP64-bound kernel sits")
 
     # end to end through the C ABI with host buffers: upload, step, download.
-    # One untimed round trip first; then every step is bracketed by events
-    # on the library's stream around the upload, the step and the download,
-    # so the record shows the host-link rates that bound this figure.
+    # fst_set_state from page-locked memory is the fused upload (3D mixed:
+    # the primitives are computed as the state arrives) and
+    # fst_rk_step_get_state copies each variable group out as soon as the
+    # last stage has finished it.  One untimed round trip first; every timed
+    # round trip is bracketed by events around the upload and around the
+    # step + download.  The plain link rates (one copy each way) and a
+    # round trip with plain copies around fst_rk_step are recorded beside it.
     n_state = int(np.prod(abi.dims(cfg)))
     host = torch.empty(n_state, dtype=torch.float64, pin_memory=True)
     host.numpy()[:] = np.asfortranarray(U0).ravel(order="F")
     L = lib()
+    L.fst_rk_step_get_state.restype = C.c_int
+    L.fst_rk_step_get_state.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t]
     ptr = C.cast(C.c_void_p(host.data_ptr()), C.POINTER(C.c_double))
 
     def round_trip(ev=None):
@@ -319,33 +325,62 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
         assert L.fst_set_state(s._ctx, ptr, n_state) == 0
         if ev:
             ev[1].record(stream)
-        assert L.fst_rk_step(s._ctx, 1) == 0
+        assert L.fst_rk_step_get_state(s._ctx, 1, ptr, n_state) == 0
         if ev:
             ev[2].record(stream)
-        assert L.fst_get_state(s._ctx, ptr, n_state) == 0
-        if ev:
-            ev[3].record(stream)
 
     round_trip()
     torch.cuda.synchronize()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(e2e_steps)]
     t0 = time.perf_counter()
     for ev in evs:
         round_trip(ev)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    e2e_ms = evs[0][0].elapsed_time(evs[-1][3])
-    h2d = [e[0].elapsed_time(e[1]) for e in evs]
-    stp = [e[1].elapsed_time(e[2]) for e in evs]
-    d2h = [e[2].elapsed_time(e[3]) for e in evs]
+    e2e_ms = evs[0][0].elapsed_time(evs[-1][2])
+    up = [e[0].elapsed_time(e[1]) for e in evs]
+    sd = [e[1].elapsed_time(e[2]) for e in evs]
     e2e_val = cells * e2e_steps / (max(e2e_ms / 1e3, wall)) / 1e6
     nbytes = n_state * 8
+    # the link on its own: one plain copy each way of the same bytes
+    dev = torch.empty(n_state, dtype=torch.float64, device="cuda")
+    link = {}
+    for name, fn in (("h2d", lambda: dev.copy_(host, non_blocking=True)),
+                     ("d2h", lambda: host.copy_(dev, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        link[name] = a.elapsed_time(b)
+    del dev
+    # the same round trip with plain copies: copy in, full step, copy out
+    seq = []
+    import os as _os
+    _os.environ["FST_NO_FUSED_UPLOAD"] = "1"
+    try:
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            assert L.fst_set_state(s._ctx, ptr, n_state) == 0
+            assert L.fst_rk_step(s._ctx, 1) == 0
+            assert L.fst_get_state(s._ctx, ptr, n_state) == 0
+            b.record(stream)
+            torch.cuda.synchronize()
+            seq.append(a.elapsed_time(b))
+    finally:
+        del _os.environ["FST_NO_FUSED_UPLOAD"]
     e2e_detail = {"timed_steps": e2e_steps, "untimed_round_trips": 1,
-                  "h2d_ms_median": statistics.median(h2d),
-                  "h2d_gbs": nbytes / (statistics.median(h2d) / 1e3) / 1e9,
-                  "d2h_ms_median": statistics.median(d2h),
-                  "d2h_gbs": nbytes / (statistics.median(d2h) / 1e3) / 1e9,
-                  "step_ms_median": statistics.median(stp),
+                  "calls": "fst_set_state + fst_rk_step_get_state, page-locked host buffer",
+                  "upload_ms_median": statistics.median(up),
+                  "step_and_download_ms_median": statistics.median(sd),
+                  "link_h2d_ms": link["h2d"], "link_h2d_gbs": nbytes / (link["h2d"] / 1e3) / 1e9,
+                  "link_d2h_ms": link["d2h"], "link_d2h_gbs": nbytes / (link["d2h"] / 1e3) / 1e9,
+                  "device_step_ms": ms / steps,
+                  "plain_copies_round_trip_ms_median": statistics.median(seq),
+                  "round_trip_ms_median": statistics.median([u + v for u, v in zip(up, sd)]),
                   "wall_s": wall, "host_buffer": "pinned (cudaHostAlloc via torch)"}
     s.close()
     return U_final, {

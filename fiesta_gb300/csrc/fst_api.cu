@@ -57,6 +57,8 @@ struct fst_ctx {
   fst_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
+  // fst_rk_step_get_state: the side stream of the overlapped download
+  MixedDownload dl{};
   int* dflag = nullptr;
   bool gen = false;       // FST_GRID_GENERALIZED
   bool grid_set = false;  // fst_set_grid has computed the metrics
@@ -515,6 +517,11 @@ void fst_destroy(fst_ctx* c) {
   if (c->Rdev) cudaFree(c->Rdev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->dl.side) {
+    cudaStreamSynchronize(c->dl.side);
+    cudaStreamDestroy(c->dl.side);
+    for (cudaEvent_t e : c->dl.ev) cudaEventDestroy(e);
+  }
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -536,10 +543,51 @@ int fst_synchronize(fst_ctx* c) {
   return device_errors(c);
 }
 
+namespace {
+// A device-visible address of host buffer U[0..n) for a kernel to read, or
+// null: both ends page-locked (cudaHostAlloc / cudaHostRegister) with
+// consistent device addresses, on a device that can also reach pageable
+// memory (so no address in between can fault).
+const double* device_view_of_host(const double* U, size_t n) {
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+  if (!pageable || n == 0) return nullptr;
+  cudaPointerAttributes a0{}, a1{};
+  if (cudaPointerGetAttributes(&a0, U) != cudaSuccess ||
+      cudaPointerGetAttributes(&a1, U + (n - 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer ||
+      !a1.devicePointer)
+    return nullptr;
+  const double* d0 = static_cast<const double*>(a0.devicePointer);
+  if (static_cast<const double*>(a1.devicePointer) != d0 + (n - 1)) return nullptr;
+  return d0;
+}
+}  // namespace
+
 int fst_set_state(fst_ctx* c, const double* U, size_t n) {
   if (!c || !U) return FST_ERR_INVALID;
   if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
   c->bm.fused_for = nullptr;  // the primitives no longer describe the state
+  if (c->cf.mode != FST_MODE_PLAIN_FP64 && c->bm.fused && !c->gen &&
+      !std::getenv("FST_NO_FUSED_UPLOAD")) {
+    if (const double* Ud = device_view_of_host(U, n)) {
+      const int k = fst_mixed_upload(c->g, c->P, c->bm, Ud, c->Ua, c->stream, &c->prof);
+      if (k >= 0) {
+        c->stats.kernel_launches += k;
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+          c->bm.fused_for = nullptr;
+          return cuda_fail(c, e, "set_state (fused upload)");
+        }
+        return FST_OK;
+      }
+    }
+  }
   cudaError_t e = cudaMemcpyAsync(c->Ua, U, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "set_state");
@@ -606,29 +654,96 @@ int fst_compute_rhs(fst_ctx* c, double* R, size_t n) {
   return FST_OK;
 }
 
+namespace {
+// One time step: preStep (BCs on cartesian grids), stage 1 into Ub (ghosts
+// copied), BCs on Ub (3D cartesian), stage 2 into Ua.  A download plan in
+// c->bm.dl applies to stage 2 only.
+int one_step(fst_ctx* c) {
+  int rc = FST_OK;
+  const bool two_d = c->g.ndim == 2;
+  // gen2d / gen3d apply no boundary conditions (src/gen2d.cpp:132-134,
+  // src/gen3d.cpp:109, 338-370)
+  if (two_d && !c->gen) rc = bcs(c, c->Ua);  // cart2d_func::preStep
+  if (!rc && !two_d && !c->gen) rc = bcs(c, c->Ua);
+  c->bm.stage = 1;
+  MixedDownload* dl = c->bm.dl;
+  c->bm.dl = nullptr;
+  if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, true);
+  c->bm.dl = dl;
+  if (!rc && !two_d && !c->gen) rc = bcs(c, c->Ub);
+  c->bm.stage = 2;
+  if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
+  if (rc) return rc;
+  c->bm.step += 1;
+  c->stats.steps += 1;
+  return FST_OK;
+}
+}  // namespace
+
 int fst_rk_step(fst_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return FST_ERR_INVALID;
   if (c->gen && !c->grid_set) return fail(c, FST_ERR_INVALID, "fst_set_grid has not been called");
   cudaEventRecord(c->ev0, c->stream);
   for (int s = 0; s < nsteps; ++s) {
-    int rc = FST_OK;
-    const bool two_d = c->g.ndim == 2;
-    // gen2d / gen3d apply no boundary conditions (src/gen2d.cpp:132-134,
-    // src/gen3d.cpp:109, 338-370)
-    if (two_d && !c->gen) rc = bcs(c, c->Ua);  // cart2d_func::preStep
-    if (!rc && !two_d && !c->gen) rc = bcs(c, c->Ua);
-    c->bm.stage = 1;
-    if (!rc) rc = stage(c, c->Ua, c->Ua, c->Ub, c->P.hdt, nullptr, true);
-    if (!rc && !two_d && !c->gen) rc = bcs(c, c->Ub);
-    c->bm.stage = 2;
-    if (!rc) rc = stage(c, c->Ub, c->Ua, c->Ua, c->P.dt, nullptr, false);
+    const int rc = one_step(c);
     if (rc) return rc;
-    c->bm.step += 1;
-    c->stats.steps += 1;
   }
   cudaEventRecord(c->ev1, c->stream);
   c->timed = nsteps > 0;
   return check_launch(c, "rk_step");
+}
+
+int fst_rk_step_get_state(fst_ctx* c, int nsteps, double* U, size_t n) {
+  if (!c || !U || nsteps < 0) return FST_ERR_INVALID;
+  if (n != (size_t)c->g.sv * c->g.nvt) return fail(c, FST_ERR_SIZE, "state size mismatch");
+  // (a copy into pageable memory returns only when it is done, which would
+  // hold back the launches behind it: overlap into page-locked memory only)
+  cudaPointerAttributes pa{};
+  if (cudaPointerGetAttributes(&pa, U) != cudaSuccess) cudaGetLastError();
+  const bool overlap = nsteps > 0 && c->cf.mode != FST_MODE_PLAIN_FP64 && c->g.ndim == 3 &&
+                       !c->gen && pa.type == cudaMemoryTypeHost;
+  if (!overlap) {
+    const int rc = fst_rk_step(c, nsteps);
+    return rc ? rc : fst_get_state(c, U, n);
+  }
+  if (!c->dl.side) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->dl.side, cudaStreamNonBlocking);
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+      e = cudaEventCreateWithFlags(&c->dl.ev[q], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(c, e, "download stream");
+  }
+  cudaEventRecord(c->ev0, c->stream);
+  int rc = FST_OK;
+  c->dl.host = U;
+  c->dl.issued = 0;
+  for (int s = 0; s < nsteps && !rc; ++s) {
+    c->bm.dl = s + 1 == nsteps ? &c->dl : nullptr;  // the last step's stage 2 copies as it goes
+    rc = one_step(c);
+  }
+  c->bm.dl = nullptr;
+  if (rc) {
+    cudaStreamSynchronize(c->dl.side);
+    return rc;
+  }
+  cudaEventRecord(c->ev1, c->stream);
+  c->timed = true;
+  // groups no kernel completed on its own: after the whole stage
+  const Geo& g = c->g;
+  struct Grp {
+    int bit, v0, nvar;
+  } grps[3] = {{FST_DL_MOMENTA, 0, 4}, {FST_DL_SPECIES, 4, g.ns}, {FST_DL_CEQ, g.nv, g.nvt - g.nv}};
+  cudaError_t e = cudaSuccess;
+  for (const Grp& q : grps) {
+    if ((c->dl.issued & q.bit) || q.nvar <= 0 || e != cudaSuccess) continue;
+    const size_t off = (size_t)g.sv * q.v0;
+    e = cudaMemcpyAsync(U + off, c->Ua + off, sizeof(double) * g.sv * q.nvar,
+                        cudaMemcpyDeviceToHost, c->stream);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->dl.side);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "rk_step_get_state");
+  return device_errors(c);
 }
 
 int fst_set_grid(fst_ctx* c, const double* nodes, size_t n) {

@@ -113,6 +113,17 @@ struct PrimSet {
   Mixed3DMaps* maps3d;
   unsigned long long* red;
 };
+// fst_rk_step_get_state: during the final stage, each variable group of
+// U_new is copied to `host` on stream `side` as soon as the last kernel that
+// writes it has run (bits of `issued`: 1 the C variables, 2 the species,
+// 4 the momenta and energy)
+struct MixedDownload {
+  double* host;
+  cudaStream_t side;
+  cudaEvent_t ev[3];
+  int issued;
+};
+constexpr int FST_DL_CEQ = 1, FST_DL_SPECIES = 2, FST_DL_MOMENTA = 4;
 struct MixedBufs {
   // Geometry of the primitive arrays.  2D: the state's.  3D: rows padded to
   // a multiple of 4 floats so that every row, plane and field starts on a
@@ -160,6 +171,8 @@ struct MixedBufs {
   bool fused;
   PrimSet alt;
   const double* fused_for;
+  // set by fst_rk_step_get_state for the final stage only
+  MixedDownload* dl;
 };
 // exchange the current primitive set with b.alt
 void fst_mixed_swap(MixedBufs& b);
@@ -200,6 +213,14 @@ int fst_hybrid_features_impl(const Geo& g, const MixedBufs& b, const MixedView& 
 int fst_hybrid_pack(MixedBufs& b, const float* h_params, cudaStream_t st);
 int fst_mixed_prims(const Geo& g, const Phys& P, const fst_config& cf, const MixedBufs& b,
                     const double* U, cudaStream_t st);
+// Fused upload (3D fused stages): copy the state from host memory the GPU can
+// read (Uh, a device-visible pointer to pinned memory) into U while computing
+// the primitives of its interior and the C-equation maxima, as the previous
+// stage's epilogue would have; the first stage then fills only the ghost
+// cells.  Returns the kernel launches, or -1 when the context's stages are
+// not fused (the caller copies instead).
+int fst_mixed_upload(const Geo& g, const Phys& P, MixedBufs& b, const double* Uh, double* U,
+                     cudaStream_t st, Prof* prof);
 
 // fst_noise.cu: the postStep noise filter on state U; `noise` holds
 // fst_noise_ints(g) ints (the indicator, then the removal's tile marks).

@@ -93,6 +93,54 @@ __global__ void __launch_bounds__(256) k_mprim3_shell(Geo g, Geo gq, Phys P,
   mprim3_cell<NS>(g, gq, P, U, O, false, i, j, k, lS, lC);
 }
 
+// Fused upload: one thread per cell in storage order (as k_mprim3).  Every
+// state value comes from host memory over the host link and goes to U; the
+// interior cells also take mprim3_vals into the current primitive set.
+template <int NS>
+__global__ void __launch_bounds__(256) k_mupload3(Geo g, Geo gq, Phys P,
+                                                  const double* __restrict__ Uh,
+                                                  double* __restrict__ U, Prim3Out O,
+                                                  unsigned long long* __restrict__ red) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  const int j = t / g.ngi, i = t - j * g.ngi, k = blockIdx.z;
+  float lS = -3.0e38f, lC = -3.0e38f;
+  if (j < g.ngj) {
+    const long long sv = g.sv;
+    const long long c = (long long)i + g.sy * j + g.sz * k;
+    const bool ceq = g.nvt > g.nv;
+    double us[NS], um[4], uc[5];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) us[s] = Uh[c + sv * (4 + s)];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) um[d] = Uh[c + sv * d];
+    if (ceq) {
+#pragma unroll
+      for (int n = 0; n < 5; ++n) uc[n] = Uh[c + sv * (g.nv + n)];
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) U[c + sv * (4 + s)] = us[s];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) U[c + sv * d] = um[d];
+    if (ceq) {
+#pragma unroll
+      for (int n = 0; n < 5; ++n) U[c + sv * (g.nv + n)] = uc[n];
+    }
+    const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
+                    k >= g.ng && k < g.ngk - g.ng;
+    if (in)
+      mprim3_vals<NS>(g, P, us, um, uc, O, (long long)i + gq.sy * j + gq.sz * k, gq.sv,
+                      red != nullptr, i, j, k, lS, lC);
+  }
+  if (red) {
+    lS = warp_maxf(lS);
+    lC = warp_maxf(lC);
+    if ((threadIdx.x & 31) == 0 && lS > -1e38f) {
+      atomicMax(&red[0], fst_key((double)lS));
+      atomicMax(&red[1], fst_key((double)lC));
+    }
+  }
+}
+
 template <int NV, bool HYB>
 __global__ void __launch_bounds__(TX * TY) k_mrhs2d(Geo g, Phys P, MixedView M,
                                                     const unsigned long long* __restrict__ red,
@@ -308,8 +356,14 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
   const bool fuse = b.fused && !Rout && !b.metf;
   const bool have = fuse && b.fused_for == Uin;
   if (!fuse) b.fused_for = nullptr;
-  if (P.ceq && !have) fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
-  if (fuse) fst_fill_keys(b.alt.red, 2, FST_KEY_LOWEST, st);
+  if (P.ceq && !have) {
+    fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
+    ++n;
+  }
+  if (fuse) {
+    fst_fill_keys(b.alt.red, 2, FST_KEY_LOWEST, st);
+    ++n;
+  }
   const MixedView M{b.Q, b.rho32, b.vel32, b.p64,  b.mu32,
                     b.nrg, b.C, b.T32, b.rho64, b.p32, b.plo};
   if (g.ndim == 3 && have) {
@@ -358,6 +412,28 @@ int fst_mixed_stage(const Geo& g, const Phys& P, const fst_config& cf, MixedBufs
     b.fused_for = Unew;
   }
   return n;
+}
+
+int fst_mixed_upload(const Geo& g, const Phys& P, MixedBufs& b, const double* Uh, double* U,
+                     cudaStream_t st, Prof* prof) {
+  if (g.ndim != 3 || !b.fused || b.metf || g.ns < 1 || g.ns > 5) return -1;
+  int n = 0;
+  if (P.ceq) fst_fill_keys(b.red, 2, FST_KEY_LOWEST, st);
+  const Prim3Out O = prim3_out(P, b, false);
+  unsigned long long* red = P.ceq ? b.red : nullptr;
+  const dim3 qg(cdiv((long long)g.ngi * g.ngj, 256), 1, g.ngk), qb(256);
+  auto launch = [&]() {
+    switch (g.ns) {
+      case 1: k_mupload3<1><<<qg, qb, 0, st>>>(g, b.gq, P, Uh, U, O, red); break;
+      case 2: k_mupload3<2><<<qg, qb, 0, st>>>(g, b.gq, P, Uh, U, O, red); break;
+      case 3: k_mupload3<3><<<qg, qb, 0, st>>>(g, b.gq, P, Uh, U, O, red); break;
+      case 4: k_mupload3<4><<<qg, qb, 0, st>>>(g, b.gq, P, Uh, U, O, red); break;
+      default: k_mupload3<5><<<qg, qb, 0, st>>>(g, b.gq, P, Uh, U, O, red); break;
+    }
+  };
+  FST_LAUNCH(prof, "mupload3d", st, n, launch());
+  b.fused_for = U;
+  return n + (P.ceq ? 1 : 0);  // and the key fill
 }
 
 int fst_mixed_secondary(const Geo& g, const Phys& P, const MixedBufs& b, const double* U,

@@ -1233,20 +1233,41 @@ void fst_mixed3d_release(MixedBufs& b) {
   b.alt.maps3d = nullptr;
 }
 
+namespace {
+// fst_rk_step_get_state: once the kernels enqueued so far have run, copy
+// variables [v0, v0 + nvar) of U to the host on the side stream
+void download_group(const Geo& g, MixedDownload* dl, int bit, int slot, const double* U, int v0,
+                    int nvar, cudaStream_t st) {
+  if (!dl || nvar <= 0) return;
+  cudaEventRecord(dl->ev[slot], st);
+  cudaStreamWaitEvent(dl->side, dl->ev[slot], 0);
+  const size_t off = (size_t)g.sv * v0;
+  cudaMemcpyAsync(dl->host + off, U + off, sizeof(double) * g.sv * nvar, cudaMemcpyDeviceToHost,
+                  dl->side);
+  dl->issued |= bit;
+}
+}  // namespace
+
 int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const MixedView& M,
                     const unsigned char* smooth, const double* Uold, double* Unew, double coef,
                     double* Rout, cudaStream_t st, Prof* prof, bool hybrid, bool fused) {
   int n = 0;
-  // cell terms first: k_mmom3d adds its face terms to what k_mcell3d wrote
-  // (on a generalized grid, the metric pressure gradient)
+  // a final stage that downloads as it goes (never with a bare RHS)
+  MixedDownload* dl = Rout ? nullptr : b.dl;
+  // cell terms before the face terms: k_mmom3d adds its face terms to what
+  // k_mcell3d wrote (on a generalized grid, the metric pressure gradient)
   if (b.metf) {
     FST_LAUNCH(prof, "gen_cell", st, n,
                fst_mixedgen_cell(g, b.gq, M, b.metf, Uold, Unew, coef, Rout, st));
   } else {
-    FST_LAUNCH(prof, "mcell3d", st, n, launch_cell(g, P, b, M, Uold, Unew, coef, Rout, st));
-    if (P.ceq)
+    // the C variables first (k_mceq3d and k_mcell3d write disjoint
+    // variables): a download of U_new starts on them soonest
+    if (P.ceq) {
       FST_LAUNCH(prof, "mceq3d", st, n,
                  launch_ceq(g, P, b, M, Uold, Unew, coef, Rout, st, fused));
+      download_group(g, dl, FST_DL_CEQ, 0, Unew, g.nv, 5, st);  // C is complete
+    }
+    FST_LAUNCH(prof, "mcell3d", st, n, launch_cell(g, P, b, M, Uold, Unew, coef, Rout, st));
   }
   // fused stages: the species kernel runs last, after the momenta and energy
   // of U_new are complete, and evaluates the next stage's primitives
@@ -1261,6 +1282,7 @@ int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const Mixed
       FST_LAUNCH(prof, nm, st, n,
                  n += launch_spec_any<false>(g, P, b, M, nullptr, Uold, Unew, coef, Rout, st,
                                              fused) - 1);
+    download_group(g, dl, FST_DL_SPECIES, 1, Unew, 4, g.ns, st);  // species complete
   };
   if (!fused) spec();
   if (hybrid)
@@ -1268,6 +1290,7 @@ int fst_mixed3d_rhs(const Geo& g, const Phys& P, const MixedBufs& b, const Mixed
                launch_mom<true>(g, P, b, M, smooth, Unew, coef, Rout, st));
   else
     FST_LAUNCH(prof, "mmom3d", st, n, launch_mom<false>(g, P, b, M, nullptr, Unew, coef, Rout, st));
+  download_group(g, dl, FST_DL_MOMENTA, 2, Unew, 0, 4, st);  // momenta and energy complete
   if (fused) spec();
   return n;
 }

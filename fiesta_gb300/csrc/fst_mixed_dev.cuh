@@ -314,11 +314,34 @@ __device__ __forceinline__ void eos3(const Phys& P, const double* us, const doub
   *sp = sqrtf((1.0f + gm1.h) * p.h * rif) + sqrtf(msq) * rif;
 }
 
-// One cell of the 3D primitive pass: loads the cell's state (every value
-// before any is used, so a thread has all its loads in flight at once),
+// One cell of the 3D primitive pass from its FP64 state values (species
+// us[0..ns), momenta and energy um[0..3], C variables uc[0..4] when O.C):
 // writes the equation of state (eos3) and the FP32 C variables, and
 // accumulates the interior maxima of the wave speed and |C_hat| when `red`
 // is set.
+template <int NS>
+__device__ __forceinline__ void mprim3_vals(const Geo& g, const Phys& P, const double* us,
+                                            const double um[4], const double uc[5],
+                                            const Prim3Out& O, long long q, long long qv,
+                                            bool red, int i, int j, int k, float& lS, float& lC) {
+  float sp;
+  eos3<NS>(P, us, um, O, q, qv, &sp);
+  if (O.C) {
+#pragma unroll
+    for (int n = 0; n < 5; ++n) O.C[q + qv * n] = d2f(uc[n]);
+  }
+  if (red) {
+    const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
+                    k >= g.ng && k < g.ngk - g.ng;
+    if (in) {
+      lS = fmaxf(lS, sp);
+      lC = fmaxf(lC, fabsf(d2f(uc[1])));
+    }
+  }
+}
+
+// mprim3_vals of cell (i, j, k) of U, every value loaded before any is used
+// (a thread has all its loads in flight at once).
 template <int NS>
 __device__ __forceinline__ void mprim3_cell(const Geo& g, const Geo& gq, const Phys& P,
                                             const double* __restrict__ U, const Prim3Out& O,
@@ -338,20 +361,7 @@ __device__ __forceinline__ void mprim3_cell(const Geo& g, const Geo& gq, const P
 #pragma unroll
     for (int n = 0; n < 5; ++n) uc[n] = U[c + sv * (P.nv + n)];
   }
-  float sp;
-  eos3<NS>(P, us, um, O, q, qv, &sp);
-  if (O.C) {
-#pragma unroll
-    for (int n = 0; n < 5; ++n) O.C[q + qv * n] = d2f(uc[n]);
-  }
-  if (red) {
-    const bool in = i >= g.ng && i < g.ngi - g.ng && j >= g.ng && j < g.ngj - g.ng &&
-                    k >= g.ng && k < g.ngk - g.ng;
-    if (in) {
-      lS = fmaxf(lS, sp);
-      lC = fmaxf(lC, fabsf(d2f(uc[1])));
-    }
-  }
+  mprim3_vals<NS>(g, P, us, um, uc, O, q, qv, red, i, j, k, lS, lC);
 }
 
 // ---------------------------------------------------------------------------

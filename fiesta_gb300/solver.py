@@ -42,6 +42,7 @@ _EXPORTS = {
     "fst_apply_bcs": (C.c_int, [C.c_void_p]),
     "fst_compute_rhs": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_rk_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "fst_rk_step_get_state": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t]),
     "fst_secondary": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t]),
     "fst_check_finite": (C.c_int, [C.c_void_p]),
     "fst_fp64_rate": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
@@ -196,6 +197,18 @@ class Solver:
 
     def rk_step(self, nsteps=1):
         self._check(lib().fst_rk_step(self._ctx, int(nsteps)), "rk_step")
+
+    def rk_step_get_state(self, nsteps=1, out=None):
+        """`nsteps` steps and the resulting state copied to host memory (out,
+        a Fortran-ordered float64 array of the state's shape, or a new one);
+        into page-locked memory the copy overlaps the end of the last step."""
+        if out is None:
+            out = np.zeros(self.shape, dtype=np.float64, order="F")
+        if out.shape != self.shape or out.dtype != np.float64 or not out.flags.f_contiguous:
+            raise ValueError("out must be a Fortran-ordered float64 array of the state's shape")
+        self._check(lib().fst_rk_step_get_state(self._ctx, int(nsteps), _dptr(out), self.n),
+                    "rk_step_get_state")
+        return out
 
     def secondary(self):
         nf = 6 if self.cfg.ndim == 3 else 5

@@ -161,6 +161,21 @@ int fst_synchronize(fst_ctx* ctx);
  * the restart reader / writer's state access. */
 int fst_set_state(fst_ctx* ctx, const double* U, size_t n);
 int fst_get_state(fst_ctx* ctx, double* U, size_t n);
+/* (3D mixed / hybrid contexts on cartesian grids with up to 5 species,
+ * U in page-locked memory the GPU can read, i.e. cudaHostAlloc'd or
+ * registered, on a device with pageable memory access such as a Grace
+ * system: fst_set_state reads U with a kernel that also computes the
+ * interior primitives on the way, so the next step skips that pass.  The
+ * result is bit for bit that of the copy.) */
+
+/* `nsteps` time steps (as fst_rk_step) and the resulting state copied to host
+ * memory U, as fst_get_state.  On 3D mixed / hybrid cartesian contexts the
+ * copy of each variable group starts during the last stage, as soon as the
+ * kernel that completes it has run (the C variables after the C-equation
+ * kernel, then the momenta and energy, then the species), so the copy
+ * overlaps the end of the step; elsewhere it follows the step.  Returns after
+ * the copy. */
+int fst_rk_step_get_state(fst_ctx* ctx, int nsteps, double* U, size_t n);
 
 /* Same, from / to device memory on the context's GPU (no host staging). */
 int fst_set_state_device(fst_ctx* ctx, const double* d_U, size_t n);
