@@ -59,6 +59,19 @@ def make_cfg(n, mode, dt=1.0):
                            eps=0.4, alpha=40.0, mode=mode)
 
 
+# The time step of the workload: dt = DT_FACTOR dx / max(|u| + c) of the
+# initial state, i.e. CFL 0.5 against twice the initial wave speed.  The
+# blasts raise the largest wave speed to 1.4-1.8x its initial value within
+# 50-200 steps; at 0.5 dx / S0 the FP64 path itself goes non-finite by step
+# 80 at 128^3 (step 60 at 256^3), at 0.25 dx / S0 both paths stay finite over
+# 200 steps at 128^3 and 256^3.
+DT_FACTOR = 0.25
+
+
+def bench_dt(cfg, U0):
+    return DT_FACTOR * cfg.dx / max_wave_speed(cfg, U0)
+
+
 def max_wave_speed(cfg, U):
     """max(|u| + c) over the interior, with the mixture gamma of the EOS."""
     ng = cfg.ng
@@ -381,6 +394,7 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
                   "device_step_ms": ms / steps,
                   "plain_copies_round_trip_ms_median": statistics.median(seq),
                   "round_trip_ms_median": statistics.median([u + v for u, v in zip(up, sd)]),
+                  "round_trip_ms": [round(e[0].elapsed_time(e[2]), 3) for e in evs],
                   "wall_s": wall, "host_buffer": "pinned (cudaHostAlloc via torch)"}
     s.close()
     return U_final, {
@@ -699,7 +713,7 @@ def cpu_sample(n_sample=128, steps=3, kind=None):
     cores = os.cpu_count() or 1
     cfg = make_cfg(n_sample, 0, 1.0)
     U0 = mixing_3d(cfg, SEED, **IC_KW)
-    cfg.dt = 0.5 * cfg.dx / max_wave_speed(cfg, U0)
+    cfg.dt = bench_dt(cfg, U0)
     if kind == "reference":
         o = Reference(cfg)
     else:
@@ -792,8 +806,7 @@ def main():
     n = a.size
     cfg0 = make_cfg(n, 0, 1.0)
     U0 = initial_conditions(cfg0, abi.IC_MIXING_3D, SEED, **IC_KW)
-    S0 = max_wave_speed(cfg0, U0)
-    dt = 0.5 * cfg0.dx / S0
+    dt = bench_dt(cfg0, U0)
     modes = [m.strip() for m in a.modes.split(",") if m.strip()]
     results, finals = {}, {}
     for m in modes:
