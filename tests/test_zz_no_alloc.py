@@ -70,6 +70,36 @@ def test_noalloc_matches_context_rhs_twice():
         assert same(R, R_ref), seed
 
 
+def test_noalloc_inside_a_stream_capture_replays_bit_for_bit():
+    """After the first call on the device, a call (C-equation on: its
+    reduction words are set by a kernel, not a host copy) sits inside a CUDA
+    graph capture in thread-local mode, and two replays give the context
+    API's RHS bit for bit."""
+    import torch
+    fn = _entry()
+    cfg = _config()
+    n = int(np.prod(abi.dims(cfg)))
+    U, R_ref = _with_ghosts(cfg, 13)
+    d_U = torch.from_numpy(U.ravel(order="F").copy()).cuda()
+    d_R = torch.empty(n, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):  # the first call on the device, outside any capture
+        assert fn(C.byref(cfg), C.c_void_p(d_U.data_ptr()), C.c_void_p(d_R.data_ptr()), n,
+                  C.c_void_p(side.cuda_stream)) == abi.FST_OK
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="thread_local"):
+        rc = fn(C.byref(cfg), C.c_void_p(d_U.data_ptr()), C.c_void_p(d_R.data_ptr()), n,
+                C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == abi.FST_OK
+    for _ in range(2):
+        d_R.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        R = d_R.cpu().numpy().reshape(abi.dims(cfg), order="F")
+        assert same(R, R_ref)
+
+
 def test_noalloc_rejects_other_configs_and_null_pointers():
     """Host-side checks only: every case returns before any launch."""
     import torch
