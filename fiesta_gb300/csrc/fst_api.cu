@@ -548,10 +548,12 @@ namespace {
 // null: both ends page-locked (cudaHostAlloc / cudaHostRegister) with
 // consistent device addresses, on a device that can also reach pageable
 // memory (so no address in between can fault).
-const double* device_view_of_host(const double* U, size_t n) {
-  int dev = 0, pageable = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+const double* device_view_of_host(const double* U, size_t n, int dev) {
+  int pageable = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
   if (!pageable || n == 0) return nullptr;
   cudaPointerAttributes a0{}, a1{};
   if (cudaPointerGetAttributes(&a0, U) != cudaSuccess ||
@@ -574,7 +576,7 @@ int fst_set_state(fst_ctx* c, const double* U, size_t n) {
   c->bm.fused_for = nullptr;  // the primitives no longer describe the state
   if (c->cf.mode != FST_MODE_PLAIN_FP64 && c->bm.fused && !c->gen &&
       !std::getenv("FST_NO_FUSED_UPLOAD")) {
-    if (const double* Ud = device_view_of_host(U, n)) {
+    if (const double* Ud = device_view_of_host(U, n, c->device)) {
       const int k = fst_mixed_upload(c->g, c->P, c->bm, Ud, c->Ua, c->stream, &c->prof);
       if (k >= 0) {
         c->stats.kernel_launches += k;

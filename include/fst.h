@@ -166,7 +166,8 @@ int fst_get_state(fst_ctx* ctx, double* U, size_t n);
  * registered, on a device with pageable memory access such as a Grace
  * system: fst_set_state reads U with a kernel that also computes the
  * interior primitives on the way, so the next step skips that pass.  The
- * result is bit for bit that of the copy.) */
+ * result is bit for bit that of the copy; FST_NO_FUSED_UPLOAD=1 in the
+ * environment selects the copy.) */
 
 /* `nsteps` time steps (as fst_rk_step) and the resulting state copied to host
  * memory U, as fst_get_state.  On 3D mixed / hybrid cartesian contexts the
