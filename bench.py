@@ -345,11 +345,20 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
     round_trip()
     torch.cuda.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(e2e_steps)]
-    t0 = time.perf_counter()
-    for ev in evs:
-        round_trip(ev)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    # the host calls are synchronous, so a pause of the Python host shows up
+    # as device idle time: no garbage collection inside the timed loop (a C
+    # or C++ caller of the same entry points has none)
+    import gc
+    gc.collect()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        for ev in evs:
+            round_trip(ev)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    finally:
+        gc.enable()
     e2e_ms = evs[0][0].elapsed_time(evs[-1][2])
     up = [e[0].elapsed_time(e[1]) for e in evs]
     sd = [e[1].elapsed_time(e[2]) for e in evs]
@@ -395,7 +404,8 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
                   "plain_copies_round_trip_ms_median": statistics.median(seq),
                   "round_trip_ms_median": statistics.median([u + v for u, v in zip(up, sd)]),
                   "round_trip_ms": [round(e[0].elapsed_time(e[2]), 3) for e in evs],
-                  "wall_s": wall, "host_buffer": "pinned (cudaHostAlloc via torch)"}
+                  "wall_s": wall, "host_buffer": "pinned (cudaHostAlloc via torch)",
+                  "python_gc": "disabled in the timed loop"}
     s.close()
     return U_final, {
         "value": value, "ms_per_step": ms / steps, "gpu_launches": launches, "hybrid": hybrid_info,
