@@ -52,10 +52,13 @@ def perturbed(U0, eps=COND_EPS, seed=1):
     return np.asfortranarray(U)
 
 
-def run_pair(cfg, U0, steps, setup=None):
-    """The GPU form's state, the FP64 oracle's, and the oracle's from the
-    perturbed initial state, after `steps` steps.  setup(solver) runs after
-    the state is set (e.g. to load classifier parameters)."""
+def run_pair(cfg, U0, steps, setup=None, reference="oracle"):
+    """The GPU form's state, the FP64 reference's, and the reference's from
+    the perturbed initial state, after `steps` steps.  setup(solver) runs
+    after the state is set (e.g. to load classifier parameters).  reference:
+    "oracle" (the CPU oracle) or "plain" (the GPU's plain FP64 path, which
+    gives the oracle's bits, tests/test_gpu_parity.py; for sizes and step
+    counts the oracle would take minutes on)."""
     m = Solver(cfg)
     m.set_state(U0)
     if setup:
@@ -66,10 +69,12 @@ def run_pair(cfg, U0, steps, setup=None):
     out = [m.get_state()]
     m.close()
     for U in (U0, perturbed(U0)):
-        o = Oracle(cref)
+        o = Oracle(cref) if reference == "oracle" else Solver(cref)
         o.set_state(U)
         o.rk_step(steps)
         out.append(o.get_state())
+        if reference != "oracle":
+            o.close()
     return out
 
 

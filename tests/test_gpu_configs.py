@@ -95,3 +95,17 @@ def test_mixing_384_mixed_step_vs_oracle():
     U, Ur, Up = run_pair(cfg, U0, 1)
     assert np.isfinite(U).all()
     check_fields(cfg, U, Ur, Up, U0)
+
+
+def test_mixing_256_hundred_steps_mixed_vs_fp64():
+    """The benchmark case itself (five-species mixing at 256^3, its time
+    step) for 100 steps: the mixed path holds every field to the bar of
+    tests/accuracy.py against the plain FP64 path over a full-length run,
+    and stays finite."""
+    from tests.accuracy import check_fields, run_pair
+    from tests.test_gpu_mixed import bench_case
+    cfg, U0 = bench_case(256)
+    U, Ur, Up = run_pair(cfg, U0, 100, reference="plain")
+    assert np.isfinite(U).all() and np.isfinite(Ur).all()
+    for v, e, tol in check_fields(cfg, U, Ur, Up, U0):
+        print(f"field {v}: rel-L2 {e:.3g} (bar {tol:.3g})")
