@@ -31,6 +31,8 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "fst_batch_dev.cuh"
 #include "fst_bc_dev.cuh"
 
@@ -284,10 +286,18 @@ std::string signature(const fst_batch* b) {
   cudaGetDevice(&dev);
   cudaGetDeviceProperties(&prop, dev);
   long long cells = 0;
-  for (auto& g : b->geos) cells += (long long)g.nci * g.ncj;
+  unsigned long long h = 1469598103934665603ull;  // FNV-1a over the case sizes, in order
+  for (auto& g : b->geos) {
+    cells += (long long)g.nci * g.ncj;
+    for (int d : {g.nci, g.ncj}) {
+      h ^= (unsigned long long)(unsigned)d;
+      h *= 1099511628211ull;
+    }
+  }
   std::ostringstream s;
-  s << prop.name << "|cases=" << b->geos.size() << "|cells=" << cells << "|nv=" << b->nv
-    << "|visc=" << b->cfgs[0].visc << "|ceq=" << b->cfgs[0].ceq;
+  s << prop.name << "|cases=" << b->geos.size() << "|cells=" << cells << "|sizes=" << std::hex
+    << h << std::dec << "|nv=" << b->nv << "|visc=" << b->cfgs[0].visc
+    << "|ceq=" << b->cfgs[0].ceq;
   return s.str();
 }
 
@@ -588,10 +598,17 @@ int fst_batch_tune(fst_batch* b, const char* json_path, int force) {
           << ", \"best_ms\": " << best << ", \"worst_ms\": " << worst << ", \"ms_per_step\": {"
           << times.str() << "}}";
     lines.push_back(entry.str());
-    std::ofstream f(json_path);
-    f << "{\"entries\": [\n";
-    for (size_t q = 0; q < lines.size(); ++q) f << lines[q] << (q + 1 < lines.size() ? ",\n" : "\n");
-    f << "]}\n";
+    // written whole to a temporary file and renamed over the store, so that a
+    // reader (or a second tuner) never sees a half-written file
+    const std::string tmp = std::string(json_path) + ".tmp" + std::to_string((long long)getpid());
+    {
+      std::ofstream f(tmp);
+      f << "{\"entries\": [\n";
+      for (size_t q = 0; q < lines.size(); ++q)
+        f << lines[q] << (q + 1 < lines.size() ? ",\n" : "\n");
+      f << "]}\n";
+    }
+    if (std::rename(tmp.c_str(), json_path) != 0) std::remove(tmp.c_str());
   }
   return FST_OK;
 }
