@@ -37,25 +37,51 @@ __device__ __forceinline__ void face_line(const Geo& g, double* __restrict__ U, 
   const long long step = ih + g.sy * jh + g.sz * kh;  // one cell outward
   const int ng = g.ng;
 
-  if (type == FST_BC_OUTFLOW) {
-    for (int v = 0; v < g.nvt; ++v)
-      for (int n = 0; n < ng; ++n)
-        U[c0 + step * (n + 1) + g.sv * v] = U[c0 - step * n + g.sv * v];
-    return;
-  }
-  // reflective, hydrostatic (reflect normal momentum) and noslip (all momenta)
-  for (int v = 0; v < g.nvt; ++v) {
-    double reflect = 1.0;
-    if (type == FST_BC_NOSLIP) {
-      if (v == 0 || v == 1 || v == 2) reflect = -1.0;
-    } else {
-      if (ih != 0 && v == 0) reflect = -1.0;
-      if (jh != 0 && v == 1) reflect = -1.0;
-      if (kh != 0 && v == 2) reflect = -1.0;
+  // The copies read only interior cells and write only ghosts, so a chunk of
+  // variables is loaded before any of it is stored: the loads are then in
+  // flight together (a store through U could alias the next load, which
+  // would otherwise serialise them).  Same values as the reference's loop.
+  constexpr int CH = 4;  // variables per chunk (with ng = 3: 12 values)
+  double x[CH][3];
+  for (int v0 = 0; v0 < g.nvt; v0 += CH) {
+#pragma unroll
+    for (int q = 0; q < CH; ++q)
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        if (v0 + q < g.nvt && n < ng) x[q][n] = U[c0 - step * n + g.sv * (v0 + q)];
+#pragma unroll
+    for (int q = 0; q < CH; ++q) {
+      const int v = v0 + q;
+      if (v >= g.nvt) break;
+      // reflective, hydrostatic (reflect normal momentum) and noslip (all momenta)
+      double reflect = 1.0;
+      if (type == FST_BC_NOSLIP) {
+        if (v == 0 || v == 1 || v == 2) reflect = -1.0;
+      } else if (type != FST_BC_OUTFLOW) {
+        if (ih != 0 && v == 0) reflect = -1.0;
+        if (jh != 0 && v == 1) reflect = -1.0;
+        if (kh != 0 && v == 2) reflect = -1.0;
+      }
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+        if (n < ng)
+          U[c0 + step * (n + 1) + g.sv * v] =
+              type == FST_BC_OUTFLOW ? x[q][n] : reflect * x[q][n];
     }
-    for (int n = 0; n < ng; ++n)
-      U[c0 + step * (n + 1) + g.sv * v] = reflect * U[c0 - step * n + g.sv * v];
   }
+  for (int n = 3; n < ng; ++n)  // more than 3 ghost layers: the plain loop
+    for (int v = 0; v < g.nvt; ++v) {
+      double reflect = 1.0;
+      if (type == FST_BC_NOSLIP) {
+        if (v == 0 || v == 1 || v == 2) reflect = -1.0;
+      } else if (type != FST_BC_OUTFLOW) {
+        if (ih != 0 && v == 0) reflect = -1.0;
+        if (jh != 0 && v == 1) reflect = -1.0;
+        if (kh != 0 && v == 2) reflect = -1.0;
+      }
+      U[c0 + step * (n + 1) + g.sv * v] = reflect * U[c0 - step * n + g.sv * v];
+    }
+  if (type == FST_BC_OUTFLOW) return;
   if (type != FST_BC_HYDROSTATIC) return;
   // linear extrapolation of internal energy (src/bc.cpp:92-123); density is
   // var(ndim+1), the first species
