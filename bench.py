@@ -404,6 +404,10 @@ def run_gpu_mode(mode_name, n, steps, warmup, U0, dt, peak_gbs, peak_kind, e2e_s
                   "plain_copies_round_trip_ms_median": statistics.median(seq),
                   "round_trip_ms_median": statistics.median([u + v for u, v in zip(up, sd)]),
                   "round_trip_ms": [round(e[0].elapsed_time(e[2]), 3) for e in evs],
+                  "upload_ms": [round(x, 3) for x in up],
+                  "step_and_download_ms": [round(x, 3) for x in sd],
+                  "median_rate": cells / (statistics.median(
+                      [u + v for u, v in zip(up, sd)]) / 1e3) / 1e6,
                   "wall_s": wall, "host_buffer": "pinned (cudaHostAlloc via torch)",
                   "python_gc": "disabled in the timed loop"}
     s.close()
@@ -765,7 +769,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--modes", default="plain,mixed,hybrid")
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     # the CPU legs: a bounded sample of the same case for the baseline beside
     # the GPU line, the full case for the reference arm (the reference's own
     # build runs ~6x slower than the oracle restatement)
