@@ -342,6 +342,10 @@ double call(fst_deck* d, const char* f, double a0, double a1, double a2, double 
   lua_State* L = d->L;
   const int top = lua_gettop(L);
   lua_getglobal(L, "fiesta");
+  if (!lua_istable(L, -1)) {  // the deck's own functions may have replaced it
+    lua_settop(L, top);
+    throw DeckError{FST_ERR_INVALID, "the deck replaced the table 'fiesta'"};
+  }
   lua_getfield(L, -1, f);
   if (lua_isnoneornil(L, -1)) {
     lua_settop(L, top);

@@ -118,6 +118,27 @@ def test_required_key_errors(tmp_path):
         lua_deck.LuaDeck(str(r))
 
 
+def test_errors_inside_the_deck_functions_are_reported(tmp_path):
+    """A deck function that fails, returns no number, or replaces the table
+    `fiesta` gives an error status and message (no Lua panic)."""
+    base = DECK_3D.split("function fiesta.initial_conditions")[0]
+    cases = {
+        "raises": ('function fiesta.initial_conditions(x, y, z, v) error("boom") end',
+                   "error running function 'initial_conditions'"),
+        "nonumber": ('function fiesta.initial_conditions(x, y, z, v) return "x" end',
+                     "should return a number"),
+        "replaced": ('function fiesta.initial_conditions(x, y, z, v) fiesta = 3; return 0 end',
+                     "replaced the table 'fiesta'"),
+    }
+    for name, (fn, msg) in cases.items():
+        p = tmp_path / f"{name}.lua"
+        p.write_text(base + fn + "\n")
+        d = lua_deck.LuaDeck(str(p))
+        with pytest.raises(lua_deck.LuaDeckError, match=msg):
+            d.initial_conditions(d.config())
+        d.close()
+
+
 def _compile_module_lua(outdir):
     from fiesta_gb300.build import DECK_LIB, LIB, build, build_deck, lua_sources
     build()
