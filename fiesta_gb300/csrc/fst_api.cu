@@ -974,8 +974,8 @@ int fst_hybrid_features(fst_ctx* c, float* d_features, unsigned char* d_labels, 
   }
   c->bm.fused_for = nullptr;
   c->stats.kernel_launches += fst_mixed_prims(c->g, c->P, c->cf, c->bm, c->Ua, c->stream);
-  const MixedView M{c->bm.Q,   c->bm.rho32, c->bm.vel32, c->bm.p64,   c->bm.mu32, c->bm.nrg,
-                    c->bm.C,   c->bm.T32,   c->bm.rho64, c->bm.p32};
+  const MixedView M{c->bm.Q, c->bm.rho32, c->bm.vel32, c->bm.p64,  c->bm.mu32, c->bm.nrg,
+                    c->bm.C, c->bm.T32,   c->bm.rho64, c->bm.p32, c->bm.plo};
   int rc = fst_hybrid_features_impl(c->bm.gq, c->bm, M, d_features, d_labels, capacity,
                                     label_ratio, count, c->stream);
   if (rc) return fail(c, rc, "feature kernels");
