@@ -131,7 +131,8 @@ def build_deck(force=False, verbose=False):
     """Compile fiesta_gb300/libfst_deck.so: the Lua deck reader
     (csrc/fst_deck.cpp, include/fst_deck.h) and the Lua 5.3 library from the
     sources lua_sources() finds (compiled where they lie, as the reference's
-    tpls/lua/CMakeLists.txt builds them: LUA_USE_LINUX).  Returns the path,
+    tpls/lua/CMakeLists.txt builds them: LUA_USE_LINUX), all without FMA
+    contraction so that x86 and Arm give the same bits.  Returns the path,
     or None when no Lua sources are present (the library is then absent)."""
     src = lua_sources()
     if src is None:
@@ -147,11 +148,14 @@ def build_deck(force=False, verbose=False):
     cmds, objs = [], []
     for u in LUA_UNITS:
         obj = os.path.join(bdir, u + ".o")
-        cmds.append(["gcc", "-O2", "-std=gnu99", "-fPIC", "-DLUA_USE_LINUX", "-w", "-c",
-                     os.path.join(src, u + ".c"), "-o", obj])
+        cmds.append(["gcc", "-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-DLUA_USE_LINUX",
+                     "-w", "-c", os.path.join(src, u + ".c"), "-o", obj])
         objs.append(obj)
     obj = os.path.join(BUILD, "fst_deck.o")
-    cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-I", src, "-c", dsrc, "-o", obj])
+    # no FMA contraction (gcc contracts by default on aarch64): the cell
+    # centres and the deck's arithmetic round as in the Python reader
+    cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", src, "-c", dsrc,
+                 "-o", obj])
     objs.append(obj)
 
     def run(cmd):
